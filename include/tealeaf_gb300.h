@@ -1,0 +1,164 @@
+/*
+ * tealeaf_gb300.h -- C ABI of the GB300 (sm_103a) TeaLeaf solve library.
+ *
+ * The library replaces the solve path of Laura7089/TeaLeaf.jl: the solver
+ * plugins called as `set.solver.solve!(chunk, set, rx, ry)`
+ * (src/TeaLeaf.jl:74) and the kernels they drive (src/kernels.jl).  A caller
+ * (the Julia shim, the Python host mirror, a C driver) owns one tl_ctx per
+ * Chunk; the context keeps every field resident in HBM across timesteps and
+ * host arrays are only borrowed for the duration of an upload/download.
+ *
+ * Conventions
+ *  - every entry point returns an int status (TL_OK == 0); tl_last_error()
+ *    gives the message of the last failure on that context;
+ *  - host field arrays use the reference's Chunk layout (src/chunk.jl:19-38):
+ *    Float64, column-major (X, Y), X = xcells + 2*halodepth, with a leading
+ *    dimension ld >= X;
+ *  - a context is not thread-safe; all work runs on the context's stream.
+ */
+#ifndef TEALEAF_GB300_H
+#define TEALEAF_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TL_API_VERSION 1
+
+typedef struct tl_ctx tl_ctx;
+
+/* status codes */
+enum {
+  TL_OK = 0,
+  TL_ERR_ARG = 1,               /* invalid argument or size                                  */
+  TL_ERR_CUDA = 2,              /* CUDA runtime error (message names the call)               */
+  TL_ERR_COEF = 3,              /* invalid coefficient: src/solvers/CG.jl:48-50, Jacobi.jl:34-36 */
+  TL_ERR_EIGEN = 4,             /* negative eigenvalue estimate: src/kernels.jl:41-43        */
+  TL_ERR_REFERENCE_THROWS = 5,  /* reference mode reached a statement where the reference raises */
+  TL_ERR_NOMEM = 6,             /* device allocation failed                                  */
+  TL_ERR_STATE = 7              /* call out of order (e.g. solve before initialise)          */
+};
+
+/* Chunk fields, in the order of the reference's Chunk struct (src/chunk.jl:24-38), plus volume (:46) */
+enum {
+  TL_DENSITY0 = 0, TL_DENSITY, TL_ENERGY0, TL_ENERGY, TL_U, TL_U0, TL_P, TL_R, TL_MI, TL_W, TL_KX, TL_KY,
+  TL_SD, TL_VOLUME, TL_NFIELDS
+};
+
+/* EXCHANGE_FIELDS (src/chunk.jl:12) */
+enum { TL_EX_DENSITY = 0, TL_EX_P, TL_EX_ENERGY0, TL_EX_ENERGY, TL_EX_U, TL_EX_SD, TL_NEX };
+
+/* semantics */
+enum {
+  TL_MODE_REFERENCE = 0,  /* the reference as written: diagonal smvp, off-by-one halo, transposed geometry */
+  TL_MODE_TEALEAF = 1     /* the intended algorithm: 5-point operator, reflective halo                    */
+};
+
+enum { TL_SOLVER_CG = 0, TL_SOLVER_CHEBY = 1, TL_SOLVER_PPCG = 2, TL_SOLVER_JACOBI = 3 };
+enum { TL_CONDUCTIVITY = 1, TL_RECIP_CONDUCTIVITY = 2 };     /* src/settings.jl:13-14 */
+enum { TL_GEOM_RECTANGULAR = 0, TL_GEOM_CIRCULAR = 1, TL_GEOM_POINT = 2 };
+enum {
+  TL_CRIT_REFERENCE = 0,  /* each solver's own test: CG sqrt|rr| < eps (CG.jl:24), others |error| < eps */
+  TL_CRIT_RELATIVE = 1    /* sqrt(rr / (u0.u0)) < eps on the recursive residual, then checked on the true one */
+};
+enum { TL_PREC_FP64 = 0, TL_PREC_FP32_IR = 1 };
+
+/* Chunk(settings) (src/chunk.jl:68-89) */
+typedef struct {
+  int xcells, ycells, halodepth;
+  int maxiters;             /* length of the cg/cheby coefficient tables */
+  double xmin, ymin, dx, dy;
+  int mode;                 /* TL_MODE_* */
+} tl_config;
+
+/* State (src/settings.jl:20-29) with the bounds already inset by the caller
+ * (src/settings.jl:159-162). */
+typedef struct {
+  double density, energy, xmin, ymin, xmax, ymax, radius;
+  int geometry;
+} tl_state;
+
+/* The Settings fields a solve reads (src/settings.jl:39-78) */
+typedef struct {
+  int solver;               /* TL_SOLVER_*                                   */
+  int coefficient;          /* TL_CONDUCTIVITY / TL_RECIP_CONDUCTIVITY       */
+  int maxiters;             /* <= tl_config.maxiters                         */
+  int presteps;             /* Cheby/PPCG CG steps before the switch         */
+  int ppcginnersteps;
+  int errorswitch;
+  double eps;
+  double epslim;
+  int criterion;            /* TL_CRIT_*                                     */
+  int precision;            /* TL_PREC_*                                     */
+  int exact;                /* 1: tealeaf mode reproduces the reference's operation order with no FMA
+                               contraction (bit-identical to the CPU restatement); 0: fused FMA kernels */
+} tl_params;
+
+typedef struct {
+  int iters;                /* trips of the solver's main loop                  */
+  int cg_iters;             /* CG iterations (presteps for Cheby/PPCG)          */
+  int inner_iters;          /* Chebyshev / PPCG iterations after the switch     */
+  int est_iters;            /* Chebyshev iteration estimate (Cheby.jl:109-118)  */
+  double error;             /* the solver loop's final error value              */
+  double eigmin, eigmax;    /* eigenvalue estimates (Cheby/PPCG)                */
+  int converged;            /* the loop ended on its convergence test           */
+  int refinements;          /* FP64 refinement passes (TL_PREC_FP32_IR)         */
+  double rel_residual;      /* ||u0 - A u|| / ||u0|| after the solve (TL_CRIT_RELATIVE) */
+} tl_result;
+
+/* Creation.  Replaces Chunk(set) (src/chunk.jl:68-89): allocates every field
+ * in HBM, zeroed, volume = dx*dy. */
+int tl_create(tl_ctx **out, const tl_config *cfg);
+int tl_destroy(tl_ctx *ctx);
+const char *tl_last_error(const tl_ctx *ctx);
+
+/* Host <-> device copies of one field (column-major (X, Y), leading dimension ld). */
+int tl_upload(tl_ctx *ctx, int field, const double *host, int ld);
+int tl_download(tl_ctx *ctx, int field, double *host, int ld);
+
+/* setchunkstate! (src/chunk.jl:122-151) */
+int tl_set_states(tl_ctx *ctx, const tl_state *states, int nstates);
+
+/* initialiseapp! (src/TeaLeaf.jl:35-44): states, halo of density, energy0,
+ * energy, then energy = energy0. */
+int tl_initialise(tl_ctx *ctx, const tl_state *states, int nstates);
+
+/* haloupdate!(chunk, set, depth[, toex][, reset]) (src/kernels.jl:146-159):
+ * nfields >= 0 marks `fields` (TL_EX_*) for exchange (clearing the others
+ * first when reset != 0) and updates them; nfields < 0 updates the fields
+ * currently marked. */
+int tl_halo_update(tl_ctx *ctx, int depth, const int *fields, int nfields, int reset);
+
+/* solve!(chunk, set, rx, ry): CG.jl:7-29, Cheby.jl:10-61, PPCG.jl:9-55,
+ * Jacobi.jl:7-30. */
+int tl_solve(tl_ctx *ctx, double rx, double ry, const tl_params *params, tl_result *result);
+
+/* solvefinished! (src/kernels.jl:166-170) */
+int tl_solve_finished(tl_ctx *ctx, int checkresult);
+
+/* fieldsummary (src/kernels.jl:119-133): out = {vol, mass, ie, temp} over the
+ * interior; temp is the reference's quantity, the other three are added. */
+int tl_field_summary(tl_ctx *ctx, double out[4]);
+
+/* copyu! (src/kernels.jl:217-220), residual! (:227-232), finalise! (:239-242) */
+int tl_copy_u(tl_ctx *ctx);
+int tl_residual(tl_ctx *ctx);
+int tl_finalise(tl_ctx *ctx);
+
+/* CG coefficient tables cgalpha[1..n], cgbeta[1..n] (src/chunk.jl:56-57) */
+int tl_get_cg_coefficients(tl_ctx *ctx, double *alpha, double *beta, int n);
+
+/* Launch layout of the deterministic reduction tree: warps per block, rows
+ * per tile, persistent blocks.  Lets a checker reproduce the summation order. */
+int tl_reduction_layout(tl_ctx *ctx, int *warps, int *rows, int *blocks);
+
+/* Wait for all work queued on the context. */
+int tl_synchronize(tl_ctx *ctx);
+
+/* Device time in milliseconds of the iteration loop of the last tl_solve. */
+int tl_last_solve_ms(tl_ctx *ctx, double *ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

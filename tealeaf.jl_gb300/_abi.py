@@ -1,0 +1,106 @@
+"""ctypes binding of libtealeaf_gb300.so (include/tealeaf_gb300.h).
+
+The library is the product: every solve runs in its sm_103a kernels.  There is
+no CPU fallback; loading fails loudly when the library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "libtealeaf_gb300.so"
+
+# status codes
+OK, ERR_ARG, ERR_CUDA, ERR_COEF, ERR_EIGEN, ERR_REFERENCE_THROWS, ERR_NOMEM, ERR_STATE = range(8)
+FIELDS = ["density0", "density", "energy0", "energy", "u", "u0", "p", "r", "mi", "w", "kx", "ky", "sd",
+          "volume"]
+EXCHANGE_FIELDS = ["density", "p", "energy0", "energy", "u", "sd"]   # src/chunk.jl:12
+MODE_REFERENCE, MODE_TEALEAF = 0, 1
+SOLVER_CG, SOLVER_CHEBY, SOLVER_PPCG, SOLVER_JACOBI = 0, 1, 2, 3
+CRIT_REFERENCE, CRIT_RELATIVE = 0, 1
+PREC_FP64, PREC_FP32_IR = 0, 1
+GEOM_RECTANGULAR, GEOM_CIRCULAR, GEOM_POINT = 0, 1, 2
+
+
+class Config(C.Structure):
+    _fields_ = [("xcells", C.c_int), ("ycells", C.c_int), ("halodepth", C.c_int), ("maxiters", C.c_int),
+                ("xmin", C.c_double), ("ymin", C.c_double), ("dx", C.c_double), ("dy", C.c_double),
+                ("mode", C.c_int)]
+
+
+class State(C.Structure):
+    _fields_ = [("density", C.c_double), ("energy", C.c_double), ("xmin", C.c_double), ("ymin", C.c_double),
+                ("xmax", C.c_double), ("ymax", C.c_double), ("radius", C.c_double), ("geometry", C.c_int)]
+
+
+class Params(C.Structure):
+    _fields_ = [("solver", C.c_int), ("coefficient", C.c_int), ("maxiters", C.c_int), ("presteps", C.c_int),
+                ("ppcginnersteps", C.c_int), ("errorswitch", C.c_int), ("eps", C.c_double),
+                ("epslim", C.c_double), ("criterion", C.c_int), ("precision", C.c_int), ("exact", C.c_int)]
+
+
+class Result(C.Structure):
+    _fields_ = [("iters", C.c_int), ("cg_iters", C.c_int), ("inner_iters", C.c_int), ("est_iters", C.c_int),
+                ("error", C.c_double), ("eigmin", C.c_double), ("eigmax", C.c_double), ("converged", C.c_int),
+                ("refinements", C.c_int), ("rel_residual", C.c_double)]
+
+
+# every symbol the header declares, with its ctypes signature
+_P = C.POINTER
+_CTX = C.c_void_p
+SIGNATURES = {
+    "tl_create": ([_P(_CTX), _P(Config)], C.c_int),
+    "tl_destroy": ([_CTX], C.c_int),
+    "tl_last_error": ([_CTX], C.c_char_p),
+    "tl_upload": ([_CTX, C.c_int, _P(C.c_double), C.c_int], C.c_int),
+    "tl_download": ([_CTX, C.c_int, _P(C.c_double), C.c_int], C.c_int),
+    "tl_set_states": ([_CTX, _P(State), C.c_int], C.c_int),
+    "tl_initialise": ([_CTX, _P(State), C.c_int], C.c_int),
+    "tl_halo_update": ([_CTX, C.c_int, _P(C.c_int), C.c_int, C.c_int], C.c_int),
+    "tl_solve": ([_CTX, C.c_double, C.c_double, _P(Params), _P(Result)], C.c_int),
+    "tl_solve_finished": ([_CTX, C.c_int], C.c_int),
+    "tl_field_summary": ([_CTX, _P(C.c_double)], C.c_int),
+    "tl_copy_u": ([_CTX], C.c_int),
+    "tl_residual": ([_CTX], C.c_int),
+    "tl_finalise": ([_CTX], C.c_int),
+    "tl_get_cg_coefficients": ([_CTX, _P(C.c_double), _P(C.c_double), C.c_int], C.c_int),
+    "tl_reduction_layout": ([_CTX, _P(C.c_int), _P(C.c_int), _P(C.c_int)], C.c_int),
+    "tl_synchronize": ([_CTX], C.c_int),
+    "tl_last_solve_ms": ([_CTX, _P(C.c_double)], C.c_int),
+}
+
+_lib = None
+
+
+class TeaLeafError(RuntimeError):
+    """A non-zero status from the library (the reference's `throw`s map here)."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(msg)
+        self.code = code
+
+
+def load(path: Path | None = None):
+    """Load the CUDA library; raises if it is missing (no fallback)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it with tealeaf.jl_gb300/build.py (the solve path has no "
+                           "CPU fallback)")
+    lib = C.CDLL(str(p))
+    for name, (args, res) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(lib, ctx, rc: int):
+    if rc:
+        msg = lib.tl_last_error(ctx)
+        raise TeaLeafError(rc, msg.decode() if msg else f"status {rc}")

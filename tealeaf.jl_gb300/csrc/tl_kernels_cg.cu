@@ -1,0 +1,336 @@
+// tl_kernels_cg.cu -- the CG iteration (src/solvers/CG.jl:32-44, 82-104).
+//
+// Reference mode: w! / ur! / p! as three passes with the reference's diagonal
+// smvp (kernels.jl:180-181) and explicitly rounded arithmetic.
+//
+// Tealeaf mode: two fused passes per iteration,
+//   step W : p' = beta*p + r (the previous iteration's p!), w = A p', p'.w
+//   step UR: u += alpha p', r -= alpha w, r.r
+// p' is written to the other buffer of a ping-pong pair because the stencil
+// reads p at the neighbours.  The depth-1 reflective halo of p' that the
+// reference refreshes every iteration (CG.jl:23) is folded into the index
+// math: a neighbour across the boundary is the cell itself.  EXACT keeps the
+// reference's operation order with no FMA (bit-identical to the CPU
+// restatement); otherwise the stencil is diag*p - kx1*pE - kx0*pW - ky1*pN -
+// ky0*pS with the diagonal read from memory and every update fused.
+#include "tl_walk.cuh"
+
+namespace tl {
+
+// ---------------------------------------------------------------------------
+// reference mode
+// ---------------------------------------------------------------------------
+
+struct OpRefW : NoSkip {
+  Fields F;
+  Geom g;
+  __device__ void cell(int i, int j, double (&acc)[1]) const {
+    const size_t c = g.at(i, j);
+    const double consum = dadd(dadd(dadd(dadd(1.0, F.kx[c + 1]), F.kx[c]), F.ky[c + g.pitch]), F.ky[c]);
+    const double pv = F.p[c];
+    const double wv = dmul(consum, pv);
+    F.w[c] = wv;
+    acc[0] = dadd(acc[0], dmul(wv, pv));
+  }
+  __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
+    for (int j = j0; j < j1; ++j) {
+      if (i0 < g.nx) cell(i0, j, acc);
+      if (i0 + 1 < g.nx) cell(i0 + 1, j, acc);
+    }
+  }
+  __device__ void fin(const double *tot) const {
+    DevScalars *sc = F.sc;
+    sc->pw = tot[0];
+    sc->alpha = ddiv(sc->rro, sc->pw);
+    F.cgalpha[sc->iter + 1] = sc->alpha;
+  }
+};
+
+// ur!: u += alpha p, r -= alpha w, then the epilogue of mainstep! and the
+// solver loop's convergence test.
+__device__ __forceinline__ void ur_epilogue(const Fields &F, double rrn, cudaGraphConditionalHandle cond,
+                                            int set_cond) {
+  DevScalars *sc = F.sc;
+  sc->rrn = rrn;
+  sc->beta = ddiv(rrn, sc->rro);
+  F.cgbeta[sc->iter + 1] = sc->beta;
+  if (!sc->stale_rro) sc->rro = rrn;
+  sc->error = rrn;
+  sc->iter += 1;
+  sc->first = 0;
+  loop_control(sc, cond, set_cond);
+}
+
+struct OpRefUR : NoSkip {
+  Fields F;
+  Geom g;
+  cudaGraphConditionalHandle cond;
+  int set_cond;
+  __device__ void cell(int i, int j, double alpha, double (&acc)[1]) const {
+    const size_t c = g.at(i, j);
+    F.u[c] = dadd(F.u[c], dmul(alpha, F.p[c]));
+    const double rv = dsub(F.r[c], dmul(alpha, F.w[c]));
+    F.r[c] = rv;
+    acc[0] = dadd(acc[0], dmul(rv, rv));
+  }
+  __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
+    const double alpha = F.sc->alpha;
+    for (int j = j0; j < j1; ++j) {
+      if (i0 < g.nx) cell(i0, j, alpha, acc);
+      if (i0 + 1 < g.nx) cell(i0 + 1, j, alpha, acc);
+    }
+  }
+  __device__ void fin(const double *tot) const { ur_epilogue(F, tot[0], cond, set_cond); }
+};
+
+struct OpRefP : NoSkip {
+  Fields F;
+  Geom g;
+  __device__ void tile(int i0, int j0, int j1, double (&)[1]) const {
+    const double beta = F.sc->beta;
+    for (int j = j0; j < j1; ++j) {
+      if (i0 < g.nx) {
+        const size_t c = g.at(i0, j);
+        F.p[c] = dadd(dmul(beta, F.p[c]), F.r[c]);
+      }
+      if (i0 + 1 < g.nx) {
+        const size_t c = g.at(i0 + 1, j);
+        F.p[c] = dadd(dmul(beta, F.p[c]), F.r[c]);
+      }
+    }
+  }
+};
+
+void launch_ref_w(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk) {
+  OpRefW op;
+  op.F = F;
+  op.g = g;
+  launch_walk<1>(st, op, wk, g.ny);
+}
+
+void launch_ref_ur(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk, cudaGraphConditionalHandle cond,
+                   int set_cond) {
+  OpRefUR op;
+  op.F = F;
+  op.g = g;
+  op.cond = cond;
+  op.set_cond = set_cond;
+  launch_walk<1>(st, op, wk, g.ny);
+}
+
+void launch_ref_p(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk) {
+  OpRefP op;
+  op.F = F;
+  op.g = g;
+  launch_walk<0>(st, op, wk, g.ny);
+}
+
+// ---------------------------------------------------------------------------
+// tealeaf mode, fused
+// ---------------------------------------------------------------------------
+
+template <bool EXACT>
+__device__ __forceinline__ double stencil(double c, double e, double w, double n, double s, double kx0, double kx1,
+                                          double ky0, double ky1, double dg) {
+  if (EXACT) {
+    const double consum = dadd(dadd(dadd(dadd(1.0, kx1), kx0), ky1), ky0);
+    double v = dmul(consum, c);
+    v = dsub(v, dadd(dmul(kx1, e), dmul(kx0, w)));
+    v = dsub(v, dadd(dmul(ky1, n), dmul(ky0, s)));
+    return v;
+  }
+  double t = dg * c;
+  t = fma(-kx1, e, t);
+  t = fma(-kx0, w, t);
+  t = fma(-ky1, n, t);
+  t = fma(-ky0, s, t);
+  return t;
+}
+
+template <bool EXACT>
+struct OpTlW {
+  Fields F;
+  Geom g;
+  const double *__restrict__ psrc;
+  double *__restrict__ pdst;
+  int guard;
+  __device__ bool skip() const { return guard && F.sc->done; }
+  __device__ void on_skip() const {}
+
+  __device__ __forceinline__ double pn1(int i, int j, double beta, bool first) const {
+    const size_t c = g.at(i, j);
+    const double pv = __ldg(psrc + c);
+    return first ? pv : axpy<EXACT>(beta, pv, __ldg(F.r + c));
+  }
+  __device__ __forceinline__ double2 pn2(int i0, int j, double beta, bool first, bool valid) const {
+    if (!valid) return make_double2(0.0, 0.0);
+    const size_t c = g.at(i0, j);
+    const double2 pv = ld2(psrc + c);
+    if (first) return pv;
+    const double2 rv = ld2(F.r + c);
+    return make_double2(axpy<EXACT>(beta, pv.x, rv.x), axpy<EXACT>(beta, pv.y, rv.y));
+  }
+
+  __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
+    const int nx = g.nx, ny = g.ny;
+    const int lane = threadIdx.x & 31;
+    const bool valid = i0 < nx;     // the lane owns cell i0
+    const bool has1 = i0 + 1 < nx;  // ... and cell i0+1
+    const bool inner = i0 + 2 < nx; // cell i0+1 has an interior east neighbour
+    const double beta = F.sc->beta;
+    const bool first = F.sc->first != 0;
+    const double2 z = make_double2(0.0, 0.0);
+
+    double2 pc = pn2(i0, j0, beta, first, valid);
+    double2 ps = (j0 > 0) ? pn2(i0, j0 - 1, beta, first, valid) : pc;  // reflect at j = 0
+    double2 kyc = valid ? ld2(F.ky + g.at(i0, j0)) : z;
+    for (int j = j0; j < j1; ++j) {
+      const double2 pnn = (j + 1 < ny) ? pn2(i0, j + 1, beta, first, valid) : pc;  // reflect at j = ny-1
+      const double2 kyn = valid ? ld2(F.ky + g.at(i0, j + 1)) : z;
+      const double2 kx2 = valid ? ld2(F.kx + g.at(i0, j)) : z;
+      const double2 dg = (!EXACT && valid) ? ld2(F.diag + g.at(i0, j)) : z;
+      double pw = __shfl_up_sync(FULL, pc.y, 1);    // p' at i0-1
+      double pe = __shfl_down_sync(FULL, pc.x, 1);  // p' at i0+2
+      double kxe = __shfl_down_sync(FULL, kx2.x, 1);  // kx at i0+2
+      if (valid) {
+        if (i0 == 0) pw = pc.x;                       // reflect at i = 0
+        else if (lane == 0) pw = pn1(i0 - 1, j, beta, first);
+        if (has1) {
+          if (!inner) {
+            pe = pc.y;                                // reflect at i = nx-1
+            kxe = __ldg(F.kx + g.at(i0 + 2, j));      // kx of the halo column
+          } else if (lane == 31) {
+            pe = pn1(i0 + 2, j, beta, first);
+            kxe = __ldg(F.kx + g.at(i0 + 2, j));
+          }
+        }
+        const double e0 = has1 ? pc.y : pc.x;
+        const double w0 = stencil<EXACT>(pc.x, e0, pw, pnn.x, ps.x, kx2.x, kx2.y, kyc.x, kyn.x, dg.x);
+        const size_t c = g.at(i0, j);
+        acc[0] = acc_mul<EXACT>(acc[0], w0, pc.x);
+        if (has1) {
+          const double w1 = stencil<EXACT>(pc.y, pe, pc.x, pnn.y, ps.y, kx2.y, kxe, kyc.y, kyn.y, dg.y);
+          acc[0] = acc_mul<EXACT>(acc[0], w1, pc.y);
+          st2(F.w + c, make_double2(w0, w1));
+          st2(pdst + c, pc);
+        } else {
+          F.w[c] = w0;
+          pdst[c] = pc.x;
+        }
+      }
+      ps = pc;
+      pc = pnn;
+      kyc = kyn;
+    }
+  }
+  __device__ void fin(const double *tot) const {
+    DevScalars *sc = F.sc;
+    sc->pw = tot[0];
+    sc->alpha = ddiv(sc->rro, sc->pw);
+    F.cgalpha[sc->iter + 1] = sc->alpha;
+  }
+};
+
+template <bool EXACT>
+struct OpTlUR {
+  Fields F;
+  Geom g;
+  const double *__restrict__ p;
+  int guard;
+  cudaGraphConditionalHandle cond;
+  int set_cond;
+  __device__ bool skip() const { return guard && F.sc->done; }
+  __device__ void on_skip() const {
+    if (set_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0u);
+  }
+  __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
+    if (i0 >= g.nx) return;
+    const bool has1 = i0 + 1 < g.nx;
+    const double alpha = F.sc->alpha;
+    for (int j = j0; j < j1; ++j) {
+      const size_t c = g.at(i0, j);
+      const double2 pv = ld2(p + c), wv = ld2(F.w + c);
+      double2 uv = ld2(F.u + c), rv = ld2(F.r + c);
+      uv.x = axpy<EXACT>(alpha, pv.x, uv.x);
+      uv.y = axpy<EXACT>(alpha, pv.y, uv.y);
+      if (EXACT) {
+        rv.x = dsub(rv.x, dmul(alpha, wv.x));
+        rv.y = dsub(rv.y, dmul(alpha, wv.y));
+      } else {
+        rv.x = fma(-alpha, wv.x, rv.x);
+        rv.y = fma(-alpha, wv.y, rv.y);
+      }
+      acc[0] = acc_mul<EXACT>(acc[0], rv.x, rv.x);
+      if (has1) {
+        acc[0] = acc_mul<EXACT>(acc[0], rv.y, rv.y);
+        st2(F.u + c, uv);
+        st2(F.r + c, rv);
+      } else {
+        F.u[c] = uv.x;
+        F.r[c] = rv.x;
+      }
+    }
+  }
+  __device__ void fin(const double *tot) const { ur_epilogue(F, tot[0], cond, set_cond); }
+};
+
+template <bool EXACT>
+struct OpTlP : NoSkip {
+  Fields F;
+  Geom g;
+  const double *psrc;
+  double *pdst;
+  __device__ void tile(int i0, int j0, int j1, double (&)[1]) const {
+    if (i0 >= g.nx) return;
+    const bool has1 = i0 + 1 < g.nx;
+    const double beta = F.sc->beta;
+    for (int j = j0; j < j1; ++j) {
+      const size_t c = g.at(i0, j);
+      const double2 pv = ld2(psrc + c), rv = ld2(F.r + c);
+      const double2 o = make_double2(axpy<EXACT>(beta, pv.x, rv.x), axpy<EXACT>(beta, pv.y, rv.y));
+      if (has1) st2(pdst + c, o);
+      else pdst[c] = o.x;
+    }
+  }
+};
+
+void launch_tl_w(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk, const double *psrc, double *pdst,
+                 int exact, int guard) {
+  if (exact) {
+    OpTlW<true> op;
+    op.F = F; op.g = g; op.psrc = psrc; op.pdst = pdst; op.guard = guard;
+    launch_walk<1>(st, op, wk, g.ny);
+  } else {
+    OpTlW<false> op;
+    op.F = F; op.g = g; op.psrc = psrc; op.pdst = pdst; op.guard = guard;
+    launch_walk<1>(st, op, wk, g.ny);
+  }
+}
+
+void launch_tl_ur(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk, const double *p, int exact,
+                  int guard, cudaGraphConditionalHandle cond, int set_cond) {
+  if (exact) {
+    OpTlUR<true> op;
+    op.F = F; op.g = g; op.p = p; op.guard = guard; op.cond = cond; op.set_cond = set_cond;
+    launch_walk<1>(st, op, wk, g.ny);
+  } else {
+    OpTlUR<false> op;
+    op.F = F; op.g = g; op.p = p; op.guard = guard; op.cond = cond; op.set_cond = set_cond;
+    launch_walk<1>(st, op, wk, g.ny);
+  }
+}
+
+void launch_tl_p(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk, const double *psrc, double *pdst,
+                 int exact) {
+  if (exact) {
+    OpTlP<true> op;
+    op.F = F; op.g = g; op.psrc = psrc; op.pdst = pdst;
+    launch_walk<0>(st, op, wk, g.ny);
+  } else {
+    OpTlP<false> op;
+    op.F = F; op.g = g; op.psrc = psrc; op.pdst = pdst;
+    launch_walk<0>(st, op, wk, g.ny);
+  }
+}
+
+}  // namespace tl

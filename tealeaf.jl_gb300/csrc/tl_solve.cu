@@ -1,0 +1,261 @@
+// tl_solve.cu -- solve!(chunk, set, rx, ry) for the CG plugin
+// (src/solvers/CG.jl:7-29) and the shared pieces of the other solvers:
+// tea_leaf_init, loop parameters, and the while-node iteration graphs.
+#include <cmath>
+#include <cstring>
+
+#include "tl_solvers.h"
+#include "tl_walk.cuh"
+
+using namespace tl;
+
+namespace {
+
+struct LoopParams {
+  double eps, epslim;
+  int maxiters, presteps, errorswitch, stale_rro, crit, switch_rule;
+};
+
+__global__ void k_set_params(DevScalars *sc, LoopParams p) {
+  sc->eps = p.eps;
+  sc->epslim = p.epslim;
+  sc->maxiters = p.maxiters;
+  sc->presteps = p.presteps;
+  sc->errorswitch = p.errorswitch;
+  sc->stale_rro = p.stale_rro;
+  sc->crit = p.crit;
+  sc->switch_rule = p.switch_rule;
+}
+
+}  // namespace
+
+int tl_set_loop_params(tl_ctx *ctx, const tl_params *prm, int switch_rule, int stale_rro) {
+  LoopParams p;
+  p.eps = prm->eps;
+  p.epslim = prm->epslim;
+  p.maxiters = prm->maxiters;
+  p.presteps = prm->presteps;
+  p.errorswitch = prm->errorswitch;
+  p.stale_rro = stale_rro;
+  p.crit = prm->criterion;
+  p.switch_rule = switch_rule;
+  k_set_params<<<1, 1, 0, ctx->stream>>>(ctx->F.sc, p);
+  CKL();
+  return TL_OK;
+}
+
+int tl_read_scalars(tl_ctx *ctx) {
+  CK(cudaMemcpyAsync(ctx->host_sc, ctx->F.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return TL_OK;
+}
+
+const Walk &tl_walk_for(tl_ctx *ctx, int exact) {
+  return (ctx->cfg.mode == TL_MODE_REFERENCE || exact) ? ctx->walk_exact : ctx->walk_fast;
+}
+
+// CG.init! (CG.jl:47-79).  Also stores the fused kernels' diagonal.
+int tl_cg_init(tl_ctx *ctx, double rx, double ry, int coefficient, int exact) {
+  if (coefficient != TL_CONDUCTIVITY && coefficient != TL_RECIP_CONDUCTIVITY) {
+    tl_set_error(ctx, "Coefficient %d is not valid (src/solvers/CG.jl:49)", coefficient);
+    return TL_ERR_COEF;
+  }
+  launch_init_pre(ctx->stream, ctx->F, ctx->g, coefficient);
+  CKL();
+  launch_init_coef(ctx->stream, ctx->F, ctx->g, rx, ry, 0, coefficient);
+  CKL();
+  if (ctx->cfg.mode == TL_MODE_TEALEAF && !exact) {
+    launch_init_diag(ctx->stream, ctx->F, ctx->g);
+    CKL();
+  }
+  launch_init_resid(ctx->stream, ctx->F, ctx->g, ctx->walk_exact, ctx->cfg.mode);
+  CKL();
+  return TL_OK;
+}
+
+// ---------------------------------------------------------------------------
+// iteration graphs
+// ---------------------------------------------------------------------------
+
+// Records the body of one while-node loop on the context stream.
+static int record_body(tl_ctx *ctx, int which, cudaGraphConditionalHandle h) {
+  const Fields &F = ctx->F;
+  const Geom &g = ctx->g;
+  cudaStream_t st = ctx->stream;
+  switch (which) {
+    case TL_GRAPH_CG_REF:
+    case TL_GRAPH_CG_REF_NOHALO: {
+      const Walk &wk = ctx->walk_exact;
+      launch_ref_w(st, F, g, wk);
+      launch_ref_ur(st, F, g, wk, h, 1);
+      launch_ref_p(st, F, g, wk);
+      if (which == TL_GRAPH_CG_REF) {
+        double *ptrs[2] = {F.p, F.u};  // haloupdate!(chunk, set, 1) with u, p marked (CG.jl:23)
+        launch_halo(st, ptrs, 2, g, 1, TL_MODE_REFERENCE);
+      }
+      break;
+    }
+    case TL_GRAPH_CG_EXACT:
+    case TL_GRAPH_CG_FAST: {
+      const int exact = which == TL_GRAPH_CG_EXACT;
+      const Walk &wk = exact ? ctx->walk_exact : ctx->walk_fast;
+      launch_tl_w(st, F, g, wk, F.p, F.pb, exact, 0);
+      launch_tl_ur(st, F, g, wk, F.pb, exact, 0, h, 0);
+      launch_tl_w(st, F, g, wk, F.pb, F.p, exact, 1);
+      launch_tl_ur(st, F, g, wk, F.p, exact, 1, h, 1);
+      break;
+    }
+    default:
+      return tl_record_solver_body(ctx, which, h);
+  }
+  return cudaGetLastError() == cudaSuccess ? TL_OK : TL_ERR_CUDA;
+}
+
+int tl_get_graph(tl_ctx *ctx, int which, cudaGraphExec_t *out) {
+  if (ctx->graph[which]) {
+    *out = ctx->graph[which];
+    return TL_OK;
+  }
+  cudaGraph_t graph = nullptr;
+  CK(cudaGraphCreate(&graph, 0));
+  cudaGraphConditionalHandle h;
+  cudaError_t e = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return tl_cuda_fail(ctx, e, "cudaGraphConditionalHandleCreate", __LINE__);
+  }
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return tl_cuda_fail(ctx, e, "cudaGraphAddNode(while)", __LINE__);
+  }
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  e = cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return tl_cuda_fail(ctx, e, "cudaStreamBeginCaptureToGraph", __LINE__);
+  }
+  int rc = record_body(ctx, which, h);
+  cudaGraph_t captured = nullptr;
+  e = cudaStreamEndCapture(ctx->stream, &captured);
+  if (rc || e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return tl_cuda_fail(ctx, e, "cudaStreamEndCapture", __LINE__);
+    tl_set_error(ctx, "recording loop body %d failed: %s", which, cudaGetErrorString(cudaGetLastError()));
+    return TL_ERR_CUDA;
+  }
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return tl_cuda_fail(ctx, e, "cudaGraphInstantiate", __LINE__);
+  ctx->graph[which] = exec;
+  *out = exec;
+  return TL_OK;
+}
+
+void tl_release_graphs(tl_ctx *ctx) {
+  for (int k = 0; k < TL_NGRAPH; ++k)
+    if (ctx->graph[k]) {
+      cudaGraphExecDestroy(ctx->graph[k]);
+      ctx->graph[k] = nullptr;
+    }
+}
+
+// Runs one loop graph, timing it with events on the context stream.
+int tl_run_graph(tl_ctx *ctx, int which, double *ms) {
+  cudaGraphExec_t exec;
+  int rc = tl_get_graph(ctx, which, &exec);
+  if (rc) return rc;
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  CK(cudaGraphLaunch(exec, ctx->stream));
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  CK(cudaEventSynchronize(ctx->ev1));
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1));
+  if (ms) *ms += t;
+  return TL_OK;
+}
+
+// ---------------------------------------------------------------------------
+// autotuned walk of the fused kernels
+// ---------------------------------------------------------------------------
+
+Walk tl_tune_walk(tl_ctx *ctx) {
+  const Geom &g = ctx->g;
+  Walk w;
+  w.warps = 8;
+  w.rows = 32;
+  const int TW = 64 * w.warps;
+  w.ntx = (g.nx + TW - 1) / TW;
+  const int nty = (g.ny + w.rows - 1) / w.rows;
+  w.tiles = w.ntx * nty;
+  const int cap = 3 * ctx->sm_count;
+  w.blocks = w.tiles < cap ? w.tiles : cap;
+  if (w.blocks < 1) w.blocks = 1;
+  return w;
+}
+
+// ---------------------------------------------------------------------------
+// CG solve!
+// ---------------------------------------------------------------------------
+
+int tl_cg_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res) {
+  const int ref = ctx->cfg.mode == TL_MODE_REFERENCE;
+  const int exact = ref || prm->exact;
+  int rc = tl_cg_init(ctx, rx, ry, prm->coefficient, exact);
+  if (rc) return rc;
+  if ((rc = tl_set_loop_params(ctx, prm, 0, 0))) return rc;
+  const int up[2] = {TL_EX_U, TL_EX_P};
+  if ((rc = tl_halo_update(ctx, 1, up, 2, 1))) return rc;   // CG.jl:11
+  if ((rc = tl_copy_u(ctx))) return rc;                     // CG.jl:12
+  ctx->last_solve_ms = 0.0;
+  if (prm->maxiters >= 1) {
+    const int which = ref ? TL_GRAPH_CG_REF : (exact ? TL_GRAPH_CG_EXACT : TL_GRAPH_CG_FAST);
+    if ((rc = tl_run_graph(ctx, which, &ctx->last_solve_ms))) return rc;
+  }
+  if ((rc = tl_read_scalars(ctx))) return rc;
+  const DevScalars &sc = *ctx->host_sc;
+  if (!ref && prm->maxiters >= 1) {
+    // the last iteration's p! and haloupdate! of u, p
+    const double *pcur = (sc.iter & 1) ? ctx->F.pb : ctx->F.p;
+    launch_tl_p(ctx->stream, ctx->F, ctx->g, tl_walk_for(ctx, exact), pcur, ctx->F.p, exact);
+    CKL();
+    if ((rc = tl_halo_update(ctx, 1, nullptr, -1, 1))) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  res->iters = sc.iter;
+  res->cg_iters = sc.iter;
+  res->error = prm->maxiters >= 1 ? sc.error : ERROR_START;
+  res->converged = sc.converged;
+  return TL_OK;
+}
+
+extern "C" int tl_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res) {
+  if (!ctx || !prm || !res) return TL_ERR_ARG;
+  memset(res, 0, sizeof *res);
+  if (!ctx->initialised) {
+    tl_set_error(ctx, "solve before initialise/set_states");
+    return TL_ERR_STATE;
+  }
+  if (prm->maxiters > ctx->cfg.maxiters) {
+    tl_set_error(ctx, "maxiters %d exceeds the context's coefficient tables (%d)", prm->maxiters, ctx->cfg.maxiters);
+    return TL_ERR_ARG;
+  }
+  switch (prm->solver) {
+    case TL_SOLVER_CG:
+      if (prm->precision == TL_PREC_FP32_IR) return tl_ir_solve(ctx, rx, ry, prm, res);
+      return tl_cg_solve(ctx, rx, ry, prm, res);
+    case TL_SOLVER_CHEBY: return tl_cheby_solve(ctx, rx, ry, prm, res);
+    case TL_SOLVER_PPCG: return tl_ppcg_solve(ctx, rx, ry, prm, res);
+    case TL_SOLVER_JACOBI: return tl_jacobi_solve(ctx, rx, ry, prm, res);
+    default:
+      tl_set_error(ctx, "unknown solver %d", prm->solver);
+      return TL_ERR_ARG;
+  }
+}

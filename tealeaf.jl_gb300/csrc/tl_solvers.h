@@ -1,0 +1,74 @@
+// tl_solvers.h -- host-side context of the library (not part of the C ABI).
+#pragma once
+
+#include "tl_internal.cuh"
+
+// Cached iteration-loop graphs.
+enum {
+  TL_GRAPH_CG_REF = 0,       // reference-mode CG step + halo of u, p
+  TL_GRAPH_CG_REF_NOHALO,    // reference-mode CG step without the halo (Cheby/PPCG presteps)
+  TL_GRAPH_CG_EXACT,         // tealeaf fused CG, reference operation order
+  TL_GRAPH_CG_FAST,          // tealeaf fused CG, FMA
+  TL_GRAPH_CHEBY_EXACT,
+  TL_GRAPH_CHEBY_FAST,
+  TL_GRAPH_JACOBI_EXACT,
+  TL_GRAPH_JACOBI_FAST,
+  TL_GRAPH_IR_INNER,         // FP32 inner CG of the refinement loop
+  TL_NGRAPH
+};
+
+struct tl_ir_state;  // FP32 refinement buffers (tl_ir.cu)
+
+struct tl_ctx {
+  tl_config cfg{};
+  tl::Geom g{};
+  int lead = 0;
+  long long field_stride = 0;
+  int device = 0, sm_count = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  tl::Walk walk_exact{}, walk_fast{};
+  double *buf = nullptr;
+  void *small = nullptr;
+  tl::Fields F{};
+  double *field_ptr[TL_NFIELDS] = {};
+  tl::DevScalars *host_sc = nullptr;
+  int toexchange[TL_NEX] = {};
+  int initialised = 0;
+  double last_solve_ms = 0.0;
+  cudaGraphExec_t graph[TL_NGRAPH] = {};
+  tl_ir_state *ir = nullptr;
+  char msg[512] = {};
+};
+
+void tl_set_error(tl_ctx *ctx, const char *fmt, ...);
+int tl_cuda_fail(tl_ctx *ctx, cudaError_t e, const char *what, int line);
+double *tl_exchange_ptr(tl_ctx *ctx, int ex);
+int tl_marked(tl_ctx *ctx, double **ptrs);
+int tl_halo_check(tl_ctx *ctx, int depth);
+tl::Walk tl_tune_walk(tl_ctx *ctx);
+void tl_release_graphs(tl_ctx *ctx);
+void tl_release_ir(tl_ctx *ctx);
+
+// shared solver pieces (tl_solve.cu)
+int tl_set_loop_params(tl_ctx *ctx, const tl_params *prm, int switch_rule, int stale_rro);
+int tl_read_scalars(tl_ctx *ctx);
+const tl::Walk &tl_walk_for(tl_ctx *ctx, int exact);
+int tl_cg_init(tl_ctx *ctx, double rx, double ry, int coefficient, int exact);
+int tl_get_graph(tl_ctx *ctx, int which, cudaGraphExec_t *out);
+int tl_run_graph(tl_ctx *ctx, int which, double *ms);
+int tl_cg_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res);
+
+// the other solver plugins (tl_solvers.cu) and the FP32 refinement (tl_ir.cu)
+int tl_record_solver_body(tl_ctx *ctx, int which, cudaGraphConditionalHandle h);
+int tl_cheby_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res);
+int tl_ppcg_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res);
+int tl_jacobi_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res);
+int tl_ir_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res);
+
+#define CK(x)                                                     \
+  do {                                                            \
+    cudaError_t e_ = (x);                                         \
+    if (e_ != cudaSuccess) return tl_cuda_fail(ctx, e_, #x, __LINE__); \
+  } while (0)
+#define CKL() CK(cudaGetLastError())

@@ -1,0 +1,119 @@
+"""GPU parity of the CG solve path, through the C ABI, against the CPU oracle.
+
+Reference mode and tealeaf `exact` mode reproduce the oracle bit for bit when
+the oracle sums in the device order (same reduction tree); against the
+reference's own summation order the iteration counts are equal and the field
+summary agrees to 1e-12 relative.  The fused FMA kernels (tealeaf, exact off)
+agree with the oracle to the tolerances written in each test.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from parity_util import CONFIG1, FIELDS, deck_text, gpu_run, oracle_run, random_deck, rel
+
+pytestmark = pytest.mark.gpu
+
+REF, TEA = O.MODE_REFERENCE, O.MODE_TEALEAF
+SUMMARY_RTOL = 1e-12          # spec field_summary tolerance (FP64)
+
+
+def _layout(chunk):
+    return chunk.reduction_layout()
+
+
+@pytest.mark.parametrize("mode", [REF, TEA])
+def test_config1_bit_exact_device_order(tl, built_lib, mode):
+    """Config 1 (10x10, 5 states, 10 steps, eps 1e-15): every field after
+    every step, every iteration count and error, bit-identical to the oracle
+    summing in the device order."""
+    chunk, res, sums, per = gpu_run(tl, CONFIG1, mode, exact=True, steps_fields=True)
+    _, ores, osums, oper = oracle_run(CONFIG1, mode, O.ORDER_DEVICE, _layout(chunk), steps_fields=True)
+    assert len(res) == len(ores) == 10
+    for tt, (g, o) in enumerate(zip(res, ores)):
+        assert g.iters == o.iters, f"step {tt + 1}"
+        assert g.error == o.error, f"step {tt + 1}"
+        for f in FIELDS:
+            np.testing.assert_array_equal(per[tt][f], oper[tt][f], err_msg=f"step {tt + 1} field {f}")
+    for g, o in zip(sums, osums):
+        assert tuple(g) == tuple(o)
+    al, be = chunk.cg_coefficients(res[-1].iters)
+    assert np.all(np.isfinite(al)) and np.all(np.isfinite(be))
+
+
+@pytest.mark.parametrize("mode", [REF, TEA])
+def test_config1_reference_order(tl, built_lib, mode):
+    """Against the reference's own summation order: iteration counts equal,
+    field summary (vol, mass, ie, temp) within 1e-12 relative."""
+    _, res, sums, _ = gpu_run(tl, CONFIG1, mode, exact=True)
+    _, ores, osums, _ = oracle_run(CONFIG1, mode, O.ORDER_REFERENCE)
+    assert [r.iters for r in res] == [r.iters for r in ores]
+    for g, o in zip(sums, osums):
+        for a, b in zip(g, o):
+            assert rel(a, b) <= SUMMARY_RTOL
+
+
+def test_config1_fused_kernels(tl, built_lib):
+    """The fused FMA CG kernels on config 1 (tealeaf mode)."""
+    _, res, sums, _ = gpu_run(tl, CONFIG1, TEA, exact=False)
+    _, ores, osums, _ = oracle_run(CONFIG1, TEA, O.ORDER_REFERENCE)
+    assert [r.iters for r in res] == [r.iters for r in ores]
+    for g, o in zip(sums, osums):
+        for a, b in zip(g, o):
+            assert rel(a, b) <= SUMMARY_RTOL
+
+
+@pytest.mark.parametrize("n,seed", [(17, 1), (64, 2), (97, 3)])
+def test_random_decks_exact(tl, built_lib, n, seed):
+    """Odd and even random-rectangle decks: bit-exact in device order."""
+    text = random_deck(n, seed, steps=2, eps=1e-12)
+    for mode in (REF, TEA):
+        chunk, res, sums, per = gpu_run(tl, text, mode, exact=True, steps_fields=True)
+        _, ores, osums, oper = oracle_run(text, mode, O.ORDER_DEVICE, _layout(chunk), steps_fields=True)
+        assert [r.iters for r in res] == [r.iters for r in ores]
+        for f in FIELDS:
+            np.testing.assert_array_equal(per[-1][f], oper[-1][f], err_msg=f"mode {mode} field {f}")
+
+
+@pytest.mark.parametrize("nx,ny,seed", [(64, 64, 5), (130, 70, 6), (33, 257, 7)])
+def test_fused_vs_oracle(tl, built_lib, nx, ny, seed):
+    """Fused FMA kernels on square and non-square tealeaf decks converging to
+    1e-10 relative: equal iteration counts, summary within 1e-12 relative,
+    u within 1e-9 relative of its maximum."""
+    text = random_deck(nx, seed, ny=ny, steps=2, eps=1e-10)
+    chunk, res, sums, per = gpu_run(tl, text, TEA, exact=False, steps_fields=True)
+    _, ores, osums, oper = oracle_run(text, TEA, O.ORDER_REFERENCE, steps_fields=True)
+    for g, o in zip(res, ores):
+        assert abs(g.iters - o.iters) <= 1
+    for g, o in zip(sums, osums):
+        for a, b in zip(g, o):
+            assert rel(a, b) <= SUMMARY_RTOL
+    u, ou = per[-1]["u"], oper[-1]["u"]
+    assert np.max(np.abs(u - ou)) <= 1e-9 * np.max(np.abs(ou))
+
+
+def test_halo_both_modes(tl, built_lib):
+    """updateface! index math: quirky in reference mode, reflective in tealeaf
+    mode, corners untouched; compared with the oracle on a patterned field."""
+    for mode in (REF, TEA):
+        text = random_deck(12, 11, steps=1)
+        s = tl.Settings.from_text(text, mode=mode)
+        chunk = tl.initialiseapp(s)
+        X, Y = chunk.size()
+        pat = np.arange(X * Y, dtype=np.float64).reshape(Y, X).T + 0.5
+        chunk.set_field("sd", pat)
+        tl.haloupdate(chunk, s, 1, ["sd"])
+        os_ = O.parse_deck(text)
+        och = O.OracleChunk(os_, O.make_opts(mode=mode))
+        och.set_field("sd", pat)
+        och.halo(1, ["sd"])
+        np.testing.assert_array_equal(chunk.field("sd"), och.field("sd"))
+
+
+def test_coefficient_error(tl, built_lib):
+    """An invalid coefficient raises like CG.jl:48-50."""
+    s = tl.Settings.from_text(deck_text(coefficient=3), mode=TEA)
+    chunk = tl.initialiseapp(s)
+    with pytest.raises(tl.TeaLeafError) as e:
+        tl.CG.solve(chunk, s, 0.004, 0.004)
+    assert e.value.code == 3
