@@ -1,0 +1,398 @@
+#!/usr/bin/env python
+"""CG time-to-solution on one GB300: the 8192^2 seeded random-rectangle deck.
+
+Workload (one "step" = one diffuse! timestep of the deck): halo of energy and
+density, the CG solve to 1e-10 relative residual (||u0 - A u|| / ||u0||, the
+true residual checked in FP64 on the device), solvefinished!.  The deck is
+synthetic and seeded: background rho=100 e=1e-4 plus 4-8 axis-aligned
+rectangles with corners uniform in [0,10]^2, rho log-uniform in [0.1, 100],
+e uniform in [0.1, 25]; dt = 0.004.  Every field (537 MB) is larger than L2,
+so no flush is needed between timed steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line.  `value` is the device time of one timestep (ms, lower
+is better) of the fastest solve variant built; `e2e` repeats the timestep
+through the C ABI with the inputs uploaded from pinned host memory and the
+result downloaded inside the timed region.  The reference arm times the CPU
+restatement of the reference solver (OpenMP over all host cores) on a bounded
+sample of the same solve.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG_DIR = ROOT / "tealeaf.jl_gb300"
+METRIC = "CG time-to-solution @1e-10 rel resid, HBM GB/s: learned+FP32-IR vs plain FP64"
+DECK_SEED = 2024
+# Mean FP64 CG iterations of timesteps 4-6 of the 8192^2 deck, measured on a
+# GB300 with the fused kernels (the CPU sample below is scaled by it).
+FP64_ITERS_8192 = 3195
+BYTES_PER_CELL_ITER = 104    # 13 FP64 words: stencil 4 + u/r update 6 + p update 3
+W_STEP_BYTES = 48            # fused p-update + stencil + p.w: read p, r, kx, ky; write p, w
+UR_STEP_BYTES = 48           # u/r update + r.r: read u, p, r, w; write u, r
+
+
+def load_package():
+    if "tealeaf_gb300" in sys.modules:
+        return sys.modules["tealeaf_gb300"]
+    spec = importlib.util.spec_from_file_location("tealeaf_gb300", PKG_DIR / "__init__.py",
+                                                  submodule_search_locations=[str(PKG_DIR)])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["tealeaf_gb300"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def load_oracle():
+    spec = importlib.util.spec_from_file_location("tealeaf_oracle_py", ROOT / "oracle" / "oracle.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def make_deck(n: int, seed: int = DECK_SEED, steps: int = 20, eps: float = 1e-10, maxiters: int = 40000) -> str:
+    rng = np.random.default_rng(seed)
+    nrect = int(rng.integers(4, 9))
+    lines = ["state 1 density=100.0 energy=0.0001"]
+    for k in range(nrect):
+        x0, x1 = sorted(float(v) for v in rng.uniform(0, 10, 2))
+        y0, y1 = sorted(float(v) for v in rng.uniform(0, 10, 2))
+        rho = float(10 ** rng.uniform(-1, 2))
+        e = float(rng.uniform(0.1, 25))
+        lines.append(f"state {k + 2} density={rho!r} energy={e!r} geometry=rectangle xmin={x0!r} xmax={x1!r} "
+                     f"ymin={y0!r} ymax={y1!r}")
+    lines += [f"x_cells={n}", f"y_cells={n}", "xmin=0.0", "ymin=0.0", "xmax=10.0", "ymax=10.0",
+              "initial_timestep=0.004", f"end_step={steps}", f"max_iters={maxiters}", "use_cg", f"eps={eps!r}",
+              "halo_depth=2", "coefficient=1", "summary_frequency=10"]
+    return "\n".join(lines) + "\n"
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_bench_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.path.read_text().splitlines():
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# the GPU arm
+# ---------------------------------------------------------------------------
+
+def gpu_setup(tl, n, precision, maxiters=40000):
+    s = tl.Settings.from_text(make_deck(n, maxiters=maxiters), mode=1, exact=False, criterion=1,
+                              precision=precision)
+    chunk = tl.initialiseapp(s)
+    return s, chunk
+
+
+def timestep(tl, chunk, s):
+    rx = s.dtinit / s.dx ** 2
+    ry = s.dtinit / s.dy ** 2
+    tl.haloupdate(chunk, s, 1, ["energy", "density"])
+    res = tl.SOLVERS[s.solver].solve(chunk, s, rx, ry)
+    tl.solvefinished(chunk, s)
+    return res
+
+
+def run_variant(tl, n, precision, steps, warmup):
+    """W untimed + K timed timesteps; each timed step bracketed by device events
+    on the library's stream."""
+    s, chunk = gpu_setup(tl, n, precision)
+    lib = chunk.lib
+    for _ in range(warmup):
+        r = timestep(tl, chunk, s)
+        if not r.converged:
+            raise RuntimeError(f"warm-up solve did not converge: {r}")
+    times, results = [], []
+    for _ in range(steps):
+        chunk.check(lib.tl_synchronize(chunk.ctx))
+        chunk.check(lib.tl_timer_start(chunk.ctx))
+        r = timestep(tl, chunk, s)
+        ms = C.c_double()
+        chunk.check(lib.tl_timer_stop(chunk.ctx, C.byref(ms)))
+        if not r.converged:
+            raise RuntimeError(f"timed solve did not converge: {r}")
+        times.append(ms.value)
+        results.append(r)
+    return s, chunk, times, results
+
+
+def run_e2e(tl, n, precision, steps, warmup):
+    """The same timestep through the C ABI with host buffers: upload energy and
+    density from pinned memory, solve, solvefinished, download energy."""
+    import torch
+    s, chunk = gpu_setup(tl, n, precision)
+    lib = chunk.lib
+    X, Y = chunk.size()
+    pinned = {nm: torch.empty((Y, X), dtype=torch.float64, pin_memory=True) for nm in ("energy", "density")}
+    out = torch.empty((Y, X), dtype=torch.float64, pin_memory=True)
+    for nm in pinned:
+        a = chunk.field(nm)
+        pinned[nm].numpy()[...] = a.T
+    fidx = {nm: ["density0", "density", "energy0", "energy", "u", "u0", "p", "r", "mi", "w", "kx", "ky", "sd",
+                 "volume"].index(nm) for nm in ("energy", "density")}
+    dptr = C.POINTER(C.c_double)
+    times, h2d, d2h = [], 0, 0
+    for k in range(warmup + steps):
+        chunk.check(lib.tl_synchronize(chunk.ctx))
+        chunk.check(lib.tl_timer_start(chunk.ctx))
+        for nm in ("energy", "density"):
+            chunk.check(lib.tl_upload(chunk.ctx, fidx[nm], C.cast(pinned[nm].data_ptr(), dptr), X))
+        r = timestep(tl, chunk, s)
+        chunk.check(lib.tl_download(chunk.ctx, fidx["energy"], C.cast(out.data_ptr(), dptr), X))
+        ms = C.c_double()
+        chunk.check(lib.tl_timer_stop(chunk.ctx, C.byref(ms)))
+        # the next step starts from this step's result, as diffuse! does
+        pinned["energy"].copy_(out)
+        if k >= warmup:
+            times.append(ms.value)
+            h2d = 2 * X * Y * 8
+            d2h = X * Y * 8
+    chunk.close()
+    return statistics.mean(times), h2d, d2h
+
+
+def kernel_roofline(tl, chunk, peaks):
+    """Average duration of the dominant fused kernels, timed alone with events."""
+    lib = chunk.lib
+    cells = chunk.settings.xcells * chunk.settings.ycells
+    out = {}
+    for k, name, b in ((0, "cg_w_step", W_STEP_BYTES), (1, "cg_ur_step", UR_STEP_BYTES)):
+        ms = C.c_double()
+        chunk.check(lib.tl_bench_kernel(chunk.ctx, k, 20, C.byref(ms)))
+        gbs = b * cells / (ms.value * 1e-3) / 1e9
+        out[name] = {"ms": ms.value, "bytes_per_cell": b, "gbs": gbs}
+    return out
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_sample(oracle, n, iters_full, threads, small=5, large=25):
+    """The oracle's tealeaf-mode CG (OpenMP over `threads`) on the same deck:
+    two bounded solves (small and large iteration caps) give the per-iteration
+    time and the set-up cost; the time-to-solution is scaled to `iters_full`."""
+    text = make_deck(n)
+    s = oracle.parse_deck(text)
+    o = oracle.make_opts(mode=oracle.MODE_TEALEAF, order=oracle.ORDER_THREADS, nthreads=threads)
+    ch = oracle.OracleChunk(s, o)
+    ch.initialise()
+    rx = s.dtinit / s.dx ** 2
+    ry = s.dtinit / s.dy ** 2
+    t = {}
+    for cap in (small, large):
+        s.maxiters = cap
+        ch.halo(1, ["energy", "density"])
+        t0 = time.perf_counter()
+        ch.solve(rx, ry)
+        t[cap] = time.perf_counter() - t0
+    per_iter = (t[large] - t[small]) / (large - small)
+    setup = max(t[small] - small * per_iter, 0.0)
+    return (setup + iters_full * per_iter) * 1e3, per_iter * 1e3, t[small] + t[large]
+
+
+def reference_arm(args):
+    """--impl reference: the CPU restatement of the reference solver (the
+    reference itself is Julia and cannot run here) on the machine's host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    oracle = load_oracle()
+    oracle.build()
+    threads = os.cpu_count() or 1
+    iters = FP64_ITERS_8192 or 5800
+    vals, per_it = [], []
+    for k in range(args.warmup + args.steps):
+        v, pi, _ = cpu_sample(oracle, args.size, iters, threads)
+        if k >= args.warmup:
+            vals.append(v)
+            per_it.append(pi)
+    value = statistics.mean(vals)
+    sample = (f"tealeaf-mode CG of the oracle on the {args.size}^2 deck: 5- and 25-iteration solves per step, "
+              f"time-to-solution scaled to {iters} iterations")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "ms", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{args.size}^2 seeded random-rectangle deck, CG to 1e-10 relative residual, "
+                                   "one timestep", "n": args.size, "seed": DECK_SEED},
+            "cpu_baseline": {"value": value, "unit": "ms", "cores": threads, "kind": "port", "sample": sample,
+                             "ms_per_iteration": statistics.mean(per_it)},
+            "e2e": {"value": value, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def gpu_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("gloo")
+    else:
+        torch.cuda.set_device(0)
+    tl = load_package()
+    peak, peak_kind = measured_peaks()
+    n = args.size
+    variants = {}
+    headline = None
+    prec = {"fp64": 0, "fp32_ir": 1}
+    order = ["fp32_ir", "fp64"] if args.variant == "all" else [args.variant]
+    with ClockSampler(local) as clk:
+        for name in order:
+            try:
+                if dist:
+                    dist.barrier()
+                s, chunk, times, results = run_variant(tl, n, prec[name], args.steps, args.warmup)
+            except tl.TeaLeafError as e:
+                variants[name] = {"error": str(e)}
+                continue
+            ms = max(times)
+            if dist:
+                t = torch.tensor([statistics.mean(times)], dtype=torch.float64)
+                dist.all_reduce(t, op=dist.ReduceOp.MAX)
+                mean_ms = float(t[0])
+            else:
+                mean_ms = statistics.mean(times)
+            iters = [r.iters for r in results]
+            loop_ms = [r.solve_ms for r in results]
+            variants[name] = {"ms_per_step": mean_ms, "max_ms": ms, "iters": iters,
+                              "rel_residual": [r.rel_residual for r in results],
+                              "loop_ms": loop_ms, "launches": [r.launches for r in results],
+                              "gbs_per_iteration": BYTES_PER_CELL_ITER * n * n * statistics.mean(iters) /
+                              (statistics.mean(loop_ms) * 1e-3) / 1e9 if name == "fp64" else None}
+            if headline is None:
+                headline = (name, chunk, results)
+            else:
+                chunk.close()
+    clocks = clk.summary()
+    if headline is None:
+        print(json.dumps({"metric": METRIC, "error": variants}))
+        return
+    hname, hchunk, hres = headline
+    roof = kernel_roofline(tl, hchunk, peak) if hname == "fp64" else None
+    hchunk.close()
+    e2e_ms, h2d, d2h = run_e2e(tl, n, prec[hname], max(1, min(args.steps, 2)), 1)
+    value = variants[hname]["ms_per_step"]
+    line = {"metric": METRIC, "value": value, "unit": "ms", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if hname == "fp64" else "f32+f64",
+            "data": "synthetic",
+            "config": {"workload": f"{n}^2 seeded random-rectangle deck, CG to 1e-10 relative residual, one "
+                                   "timestep (halo, solve, solvefinished)", "n": n, "seed": DECK_SEED,
+                       "variant": hname, "l2": "every field (537 MB at 8192^2) is larger than L2; no flush"},
+            "clocks": clocks,
+            "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(sum(r.launches for r in hres) + 6 * len(hres)),
+            "variants": variants}
+    if roof:
+        dom = max(roof.values(), key=lambda d: d["ms"])
+        dname = [k for k, v in roof.items() if v is dom][0]
+        line["roofline"] = {"bound": "hbm", "kernel": dname, "achieved": dom["gbs"], "peak": peak,
+                            "unit": "GB/s", "frac": dom["gbs"] / peak, "traffic": None,
+                            "peak_kind": peak_kind, "kernels": roof}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        oracle = load_oracle()
+        oracle.build()
+        threads = os.cpu_count() or 1
+        iters = statistics.mean(variants["fp64"]["iters"]) if "fp64" in variants and "iters" in variants["fp64"] \
+            else (FP64_ITERS_8192 or 5800)
+        v, pi, wall = cpu_sample(oracle, n, iters, threads)
+        line["cpu_baseline"] = {"value": v, "unit": "ms", "cores": threads, "kind": "port",
+                                "sample": f"oracle tealeaf-mode CG, {n}^2 deck, 5- and 25-iteration solves "
+                                          f"({wall:.1f} s), scaled to {iters:.0f} iterations",
+                                "ms_per_iteration": pi}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--size", type=int, default=8192)
+    ap.add_argument("--variant", default="all", choices=["all", "fp64", "fp32_ir"])
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

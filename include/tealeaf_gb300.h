@@ -103,7 +103,8 @@ typedef struct {
   double eigmin, eigmax;    /* eigenvalue estimates (Cheby/PPCG)                */
   int converged;            /* the loop ended on its convergence test           */
   int refinements;          /* FP64 refinement passes (TL_PREC_FP32_IR)         */
-  double rel_residual;      /* ||u0 - A u|| / ||u0|| after the solve (TL_CRIT_RELATIVE) */
+  double rel_residual;      /* ||u0 - A u|| / ||u0|| after the solve (TL_CRIT_RELATIVE), else -1 */
+  int launches;             /* kernels this solve launched (graph-body kernels counted per trip) */
 } tl_result;
 
 /* Creation.  Replaces Chunk(set) (src/chunk.jl:68-89): allocates every field
@@ -157,6 +158,17 @@ int tl_synchronize(tl_ctx *ctx);
 
 /* Device time in milliseconds of the iteration loop of the last tl_solve. */
 int tl_last_solve_ms(tl_ctx *ctx, double *ms);
+
+/* A device timer on the context stream (CUDA events): stop returns the
+ * milliseconds since start. */
+int tl_timer_start(tl_ctx *ctx);
+int tl_timer_stop(tl_ctx *ctx, double *ms);
+
+/* Times `reps` back-to-back launches of one fused iteration kernel (0: the CG
+ * p-update + stencil + p.w step, 1: the u/r update + r.r step, 2: the FP32
+ * stencil step, 3: the FP32 update step) on the current fields; for roofline
+ * measurements. */
+int tl_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch);
 
 #ifdef __cplusplus
 }

@@ -52,6 +52,7 @@ class SolveResult:
     refinements: int
     rel_residual: float
     solve_ms: float
+    launches: int
 
 
 class Chunk:
@@ -233,7 +234,7 @@ def _solve(chunk: Chunk, settings: Settings, rx: float, ry: float, solver: int) 
     else:
         settings.toexchange["u"] = True
     r = SolveResult(res.iters, res.cg_iters, res.inner_iters, res.est_iters, res.error, res.eigmin, res.eigmax,
-                    bool(res.converged), res.refinements, res.rel_residual, ms.value)
+                    bool(res.converged), res.refinements, res.rel_residual, ms.value, res.launches)
     log.info("solve complete iters=%d error=%r", r.iters, r.error)
     return r
 

@@ -43,7 +43,7 @@ class Params(C.Structure):
 class Result(C.Structure):
     _fields_ = [("iters", C.c_int), ("cg_iters", C.c_int), ("inner_iters", C.c_int), ("est_iters", C.c_int),
                 ("error", C.c_double), ("eigmin", C.c_double), ("eigmax", C.c_double), ("converged", C.c_int),
-                ("refinements", C.c_int), ("rel_residual", C.c_double)]
+                ("refinements", C.c_int), ("rel_residual", C.c_double), ("launches", C.c_int)]
 
 
 # every symbol the header declares, with its ctypes signature
@@ -68,6 +68,9 @@ SIGNATURES = {
     "tl_reduction_layout": ([_CTX, _P(C.c_int), _P(C.c_int), _P(C.c_int)], C.c_int),
     "tl_synchronize": ([_CTX], C.c_int),
     "tl_last_solve_ms": ([_CTX, _P(C.c_double)], C.c_int),
+    "tl_timer_start": ([_CTX], C.c_int),
+    "tl_timer_stop": ([_CTX, _P(C.c_double)], C.c_int),
+    "tl_bench_kernel": ([_CTX, C.c_int, C.c_int, _P(C.c_double)], C.c_int),
 }
 
 _lib = None

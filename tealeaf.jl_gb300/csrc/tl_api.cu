@@ -84,6 +84,8 @@ extern "C" int tl_create(tl_ctx **out, const tl_config *cfg) {
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
   CK(cudaEventCreate(&ctx->ev0));
   CK(cudaEventCreate(&ctx->ev1));
+  CK(cudaEventCreate(&ctx->tev0));
+  CK(cudaEventCreate(&ctx->tev1));
 
   ctx->walk_exact = make_walk(g.nx, g.ny, EXACT_WARPS, EXACT_ROWS, 2 * ctx->sm_count);
   ctx->walk_fast = tl_tune_walk(ctx);
@@ -133,6 +135,8 @@ extern "C" int tl_destroy(tl_ctx *ctx) {
   if (ctx->host_sc) cudaFreeHost(ctx->host_sc);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->tev0) cudaEventDestroy(ctx->tev0);
+  if (ctx->tev1) cudaEventDestroy(ctx->tev1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   tl_release_ir(ctx);
   delete ctx;
@@ -345,5 +349,43 @@ extern "C" int tl_synchronize(tl_ctx *ctx) {
 extern "C" int tl_last_solve_ms(tl_ctx *ctx, double *ms) {
   if (!ctx || !ms) return TL_ERR_ARG;
   *ms = ctx->last_solve_ms;
+  return TL_OK;
+}
+
+extern "C" int tl_timer_start(tl_ctx *ctx) {
+  if (!ctx) return TL_ERR_ARG;
+  CK(cudaEventRecord(ctx->tev0, ctx->stream));
+  return TL_OK;
+}
+
+extern "C" int tl_timer_stop(tl_ctx *ctx, double *ms) {
+  if (!ctx || !ms) return TL_ERR_ARG;
+  CK(cudaEventRecord(ctx->tev1, ctx->stream));
+  CK(cudaEventSynchronize(ctx->tev1));
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, ctx->tev0, ctx->tev1));
+  *ms = t;
+  return TL_OK;
+}
+
+extern "C" int tl_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch) {
+  if (!ctx || !ms_per_launch || reps < 1 || ctx->cfg.mode != TL_MODE_TEALEAF) return TL_ERR_ARG;
+  const Fields &F = ctx->F;
+  const Walk &wk = ctx->walk_fast;
+  if (kernel >= 2) return tl_ir_bench_kernel(ctx, kernel, reps, ms_per_launch);
+  if (kernel < 0) return TL_ERR_ARG;
+  launch_init_diag(ctx->stream, F, ctx->g);
+  CKL();
+  CK(cudaEventRecord(ctx->tev0, ctx->stream));
+  for (int k = 0; k < reps; ++k) {
+    if (kernel == 0) launch_tl_w(ctx->stream, F, ctx->g, wk, (k & 1) ? F.pb : F.p, (k & 1) ? F.p : F.pb, 0, 0);
+    else launch_tl_ur(ctx->stream, F, ctx->g, wk, F.pb, 0, 0, 0, 0);
+  }
+  CKL();
+  CK(cudaEventRecord(ctx->tev1, ctx->stream));
+  CK(cudaEventSynchronize(ctx->tev1));
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, ctx->tev0, ctx->tev1));
+  *ms_per_launch = t / reps;
   return TL_OK;
 }

@@ -94,6 +94,7 @@ void launch_copyu(cudaStream_t st, const Fields &F, const Geom &g, const Walk &w
 void launch_residual(cudaStream_t st, const Fields &F, const Geom &g, int mode);
 void launch_finalise(cudaStream_t st, const Fields &F, const Geom &g);
 void launch_summary(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk);
+void launch_true_resid(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk, int mode, int write);
 
 // CG iteration kernels.  `cond` is the while-node handle (0 when not in a graph).
 void launch_ref_w(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk);

@@ -370,6 +370,47 @@ struct OpSummary : NoSkip {
   }
 };
 
+// The true residual t = u0 - A u (reference operation order, halo of u read
+// from memory): sum t^2 into red[0]; with `write` also r = t, p = t (the
+// restart of a CG whose recursive residual drifted from the true one).
+struct OpTrueResid : NoSkip {
+  Fields F;
+  Geom g;
+  int mode, write;
+  __device__ void cell(int i, int j, double (&acc)[1]) const {
+    const size_t c = g.at(i, j);
+    const double t = dsub(F.u0[c], smvp_exact(F, g, F.u, c, mode));
+    if (write) {
+      F.r[c] = t;
+      F.p[c] = t;
+    }
+    acc[0] = dadd(acc[0], dmul(t, t));
+  }
+  __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
+    for (int j = j0; j < j1; ++j) {
+      if (i0 < g.nx) cell(i0, j, acc);
+      if (i0 + 1 < g.nx) cell(i0 + 1, j, acc);
+    }
+  }
+  __device__ void fin(const double *tot) const {
+    F.sc->red[0] = tot[0];
+    if (write) {
+      F.sc->rro = tot[0];
+      F.sc->first = 1;
+      F.sc->done = 0;
+    }
+  }
+};
+
+void launch_true_resid(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk, int mode, int write) {
+  OpTrueResid op;
+  op.F = F;
+  op.g = g;
+  op.mode = mode;
+  op.write = write;
+  launch_walk<1>(st, op, wk, g.ny);
+}
+
 void launch_summary(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk) {
   OpSummary op;
   op.F = F;

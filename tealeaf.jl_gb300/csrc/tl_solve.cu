@@ -205,34 +205,66 @@ Walk tl_tune_walk(tl_ctx *ctx) {
 // CG solve!
 // ---------------------------------------------------------------------------
 
+// Relative criterion: the loop stops on sqrt(rr / u0.u0) < eps for the
+// recursive residual; the true residual u0 - A u is then measured and, if it
+// has drifted above eps, CG restarts from it (r = p = u0 - A u) within the
+// remaining iteration budget.
+static int true_residual(tl_ctx *ctx, int write, double *rr) {
+  launch_true_resid(ctx->stream, ctx->F, ctx->g, ctx->walk_exact, ctx->cfg.mode, write);
+  ctx->launches += 1;
+  CKL();
+  int rc = tl_read_scalars(ctx);
+  if (rc) return rc;
+  *rr = ctx->host_sc->red[0];
+  return TL_OK;
+}
+
 int tl_cg_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res) {
   const int ref = ctx->cfg.mode == TL_MODE_REFERENCE;
   const int exact = ref || prm->exact;
   int rc = tl_cg_init(ctx, rx, ry, prm->coefficient, exact);
   if (rc) return rc;
+  ctx->launches += exact ? 3 : 4;
   if ((rc = tl_set_loop_params(ctx, prm, 0, 0))) return rc;
   const int up[2] = {TL_EX_U, TL_EX_P};
   if ((rc = tl_halo_update(ctx, 1, up, 2, 1))) return rc;   // CG.jl:11
   if ((rc = tl_copy_u(ctx))) return rc;                     // CG.jl:12
+  ctx->launches += 3;
   ctx->last_solve_ms = 0.0;
-  if (prm->maxiters >= 1) {
-    const int which = ref ? TL_GRAPH_CG_REF : (exact ? TL_GRAPH_CG_EXACT : TL_GRAPH_CG_FAST);
+  const int which = ref ? TL_GRAPH_CG_REF : (exact ? TL_GRAPH_CG_EXACT : TL_GRAPH_CG_FAST);
+  double rel = -1.0;
+  int ran = 0;
+  for (int restart = 0; restart < 8 && prm->maxiters >= 1; ++restart) {
+    const int before = ctx->host_sc->iter;
     if ((rc = tl_run_graph(ctx, which, &ctx->last_solve_ms))) return rc;
+    if ((rc = tl_read_scalars(ctx))) return rc;
+    const int trips = ctx->host_sc->iter - (restart ? before : 0);
+    ctx->launches += ref ? 4LL * trips : 4LL * ((trips + 1) / 2);
+    ran = 1;
+    if (!ref) {
+      // the last iteration's p! and haloupdate! of u, p
+      const double *pcur = (ctx->host_sc->iter & 1) ? ctx->F.pb : ctx->F.p;
+      launch_tl_p(ctx->stream, ctx->F, ctx->g, tl_walk_for(ctx, exact), pcur, ctx->F.p, exact);
+      CKL();
+      if ((rc = tl_halo_update(ctx, 1, nullptr, -1, 1))) return rc;
+      ctx->launches += 2;
+    }
+    if (prm->criterion != TL_CRIT_RELATIVE) break;
+    double tr;
+    if ((rc = true_residual(ctx, 0, &tr))) return rc;
+    const double bb = ctx->host_sc->bb;
+    rel = bb > 0 ? sqrt(tr / bb) : sqrt(tr);
+    if (rel < prm->eps || ref || ctx->host_sc->iter >= prm->maxiters) break;
+    if ((rc = true_residual(ctx, 1, &tr))) return rc;  // restart from the true residual
   }
   if ((rc = tl_read_scalars(ctx))) return rc;
   const DevScalars &sc = *ctx->host_sc;
-  if (!ref && prm->maxiters >= 1) {
-    // the last iteration's p! and haloupdate! of u, p
-    const double *pcur = (sc.iter & 1) ? ctx->F.pb : ctx->F.p;
-    launch_tl_p(ctx->stream, ctx->F, ctx->g, tl_walk_for(ctx, exact), pcur, ctx->F.p, exact);
-    CKL();
-    if ((rc = tl_halo_update(ctx, 1, nullptr, -1, 1))) return rc;
-    CK(cudaStreamSynchronize(ctx->stream));
-  }
   res->iters = sc.iter;
   res->cg_iters = sc.iter;
-  res->error = prm->maxiters >= 1 ? sc.error : ERROR_START;
-  res->converged = sc.converged;
+  res->error = ran ? sc.error : ERROR_START;
+  res->converged = ran && (prm->criterion == TL_CRIT_RELATIVE ? (rel >= 0 && rel < prm->eps) : sc.converged);
+  res->rel_residual = rel;
+  res->launches = (int)ctx->launches;
   return TL_OK;
 }
 
@@ -247,6 +279,7 @@ extern "C" int tl_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm,
     tl_set_error(ctx, "maxiters %d exceeds the context's coefficient tables (%d)", prm->maxiters, ctx->cfg.maxiters);
     return TL_ERR_ARG;
   }
+  ctx->launches = 0;
   switch (prm->solver) {
     case TL_SOLVER_CG:
       if (prm->precision == TL_PREC_FP32_IR) return tl_ir_solve(ctx, rx, ry, prm, res);

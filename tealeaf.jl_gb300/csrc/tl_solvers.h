@@ -36,6 +36,8 @@ struct tl_ctx {
   int toexchange[TL_NEX] = {};
   int initialised = 0;
   double last_solve_ms = 0.0;
+  long long launches = 0;     // kernels launched by the current solve
+  cudaEvent_t tev0 = nullptr, tev1 = nullptr;  // user timer
   cudaGraphExec_t graph[TL_NGRAPH] = {};
   tl_ir_state *ir = nullptr;
   char msg[512] = {};
@@ -65,6 +67,7 @@ int tl_cheby_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_r
 int tl_ppcg_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res);
 int tl_jacobi_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res);
 int tl_ir_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res);
+int tl_ir_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch);
 
 #define CK(x)                                                     \
   do {                                                            \
