@@ -170,6 +170,30 @@ int tl_timer_stop(tl_ctx *ctx, double *ms);
  * measurements. */
 int tl_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch);
 
+/* Field summary {vol, mass, ie, temp} of caller-owned device arrays, with no
+ * device allocation by the library.  No counterpart in the reference: it is
+ * for callers that cannot let a library call cudaMalloc, such as a host
+ * framework that owns all device memory through its own pool and hands
+ * libraries ready-made buffers, or a driver that must not pay for the device
+ * synchronisation that cudaFree implies.
+ *
+ * volume, density, energy, u: device pointers to element (0, 0) of pitched
+ * (X, Y) arrays, X = xcells + 2*halodepth, `pitch` doubles between columns;
+ * out: device pointer to 4 doubles; stream: a cudaStream_t (NULL = legacy
+ * default stream); err/errlen: optional buffer for the error message.
+ * Limits: at most 2147483647 interior cells per call; larger sizes are
+ * rejected with TL_ERR_ARG.
+ * The reduction scratch (4 x 1024 block partials and a ticket, about 33 KB)
+ * is a static device array: each GPU that loads the library holds it until
+ * the process exits.  The first call on each device looks up its address
+ * (cudaGetSymbolAddress) with that device current, so make that first call
+ * before any stream capture.  All calls on a device share the scratch: calls
+ * that overlap on the GPU (different streams, no ordering) race and give
+ * wrong sums.  The call is asynchronous on `stream`. */
+int tl_field_summary_noalloc(const double *volume, const double *density, const double *energy, const double *u,
+                             int xcells, int ycells, int halodepth, long long pitch, double *out, void *stream,
+                             char *err, int errlen);
+
 #ifdef __cplusplus
 }
 #endif
