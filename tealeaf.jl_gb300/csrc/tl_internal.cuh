@@ -57,6 +57,8 @@ struct DevScalars {
   int iter_base;        // 1-based loop index of this loop's first trip minus 1
   int cheby_iters, est_iters, calc_every;  // Chebyshev loop bookkeeping
   int first;            // the next fused CG step starts from p itself (no beta update)
+  double rr_ref;        // FP32 refinement: r.r at the last refinement
+  double delta2;        // FP32 refinement: refine once r.r < delta2 * rr_ref
 };
 
 // Device pointers of one context, passed to kernels by value.

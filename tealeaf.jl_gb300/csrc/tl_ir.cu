@@ -1,14 +1,560 @@
-// tl_ir.cu -- FP32 inner CG inside FP64 iterative refinement.
+// tl_ir.cu -- CG with FP32 inner sweeps inside FP64 refinement.
+//
+// The inner iteration is CG on FP32 vectors (p, r, w and the correction x)
+// with FP32 Kx/Ky; its dots multiply the FP32 operands exactly in FP64 and
+// accumulate in FP64.  Whenever the FP32 residual has dropped by a factor
+// delta since the last refinement, or claims convergence, the loop returns to
+// a refinement step done entirely in FP64:
+//     u += x;  x = 0;  r = u0 - A u (true residual);  test ||r|| / ||u0||.
+// The FP32 residual is then replaced by the true one and the search
+// direction is kept (the reliable-update form of iterative refinement), so
+// the Krylov space built so far is not thrown away.
+//
+// FP32 arrays: pitched like the FP64 fields, 32 floats per pitch unit, first
+// interior cell of each row 128-byte aligned; each lane owns 4 consecutive
+// cells (one float4).  The FP32 stencil uses the difference form
+// w = p + kx1 (p - pE) + kx0 (p - pW) + ky1 (p - pN) + ky0 (p - pS), which
+// keeps the identity term exact where the large coupling terms cancel.
+#include <cmath>
+#include <cstring>
+#include <new>
+
 #include "tl_solvers.h"
+#include "tl_walk.cuh"
 
-void tl_release_ir(tl_ctx *ctx) { (void)ctx; }
+using namespace tl;
 
-int tl_ir_solve(tl_ctx *ctx, double, double, const tl_params *, tl_result *) {
-  tl_set_error(ctx, "FP32 refinement not built yet");
-  return TL_ERR_ARG;
+struct tl_ir_state {
+  float *buf = nullptr;
+  long long pitch = 0, lead = 0, stride = 0;
+  float *kx = nullptr, *ky = nullptr, *p = nullptr, *pb = nullptr, *r = nullptr, *w = nullptr, *x = nullptr;
+  Walk walk{};
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // p in the first / second buffer
+};
+
+namespace {
+
+constexpr double IR_DELTA = 0.1;  // refine when ||r32|| < delta * ||r at the last refinement||
+
+struct G32 {
+  int nx, ny, hd, X, Y;
+  long long pitch;
+  __host__ __device__ __forceinline__ size_t at(int i, int j) const {
+    return (size_t)(hd + i) + (size_t)(hd + j) * (size_t)pitch;
+  }
+};
+
+struct IrPtrs {
+  float *kx, *ky, *r, *w, *x;
+};
+
+__device__ __forceinline__ float4 ld4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
+__device__ __forceinline__ void st4(float *p, float4 v) { *reinterpret_cast<float4 *>(p) = v; }
+__device__ __forceinline__ float comp(const float4 &v, int k) { return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w; }
+
+// Walk with four cells per lane: tile = 128*warps columns x rows.
+template <class Op>
+__global__ void __launch_bounds__(256) k_walk32(const Op op, const Walk wk, const int ny) {
+  if (op.skip()) {
+    op.on_skip();
+    return;
+  }
+  double acc[1] = {0.0};
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int TW = 128 * wk.warps;
+  for (int t = blockIdx.x; t < wk.tiles; t += gridDim.x) {
+    const int tx = t % wk.ntx, ty = t / wk.ntx;
+    const int i0 = tx * TW + warp * 128 + 4 * lane;
+    const int j0 = ty * wk.rows;
+    const int j1 = min(j0 + wk.rows, ny);
+    op.tile(i0, j0, j1, acc);
+  }
+  if (Op::REDUCES) finish_reduction<1>(acc, op);
 }
 
-int tl_ir_bench_kernel(tl_ctx *ctx, int, int, double *) {
-  tl_set_error(ctx, "FP32 kernels not built yet");
-  return TL_ERR_ARG;
+// W step: p' = beta*p + r (or p on the first step), w = A32 p', p'.w
+struct OpIrW {
+  static constexpr bool REDUCES = true;
+  Fields F;  // scalars, partials, counter
+  G32 g;
+  IrPtrs q;
+  const float *__restrict__ psrc;
+  float *__restrict__ pdst;
+  int guard;
+  __device__ bool skip() const { return guard && F.sc->done; }
+  __device__ void on_skip() const {}
+
+  __device__ __forceinline__ float pn1(int i, int j, float beta, bool first) const {
+    const size_t c = g.at(i, j);
+    const float pv = __ldg(psrc + c);
+    return first ? pv : fmaf(beta, pv, __ldg(q.r + c));
+  }
+  __device__ __forceinline__ float4 pn4(int i0, int j, float beta, bool first, bool valid) const {
+    if (!valid) return make_float4(0.f, 0.f, 0.f, 0.f);
+    const size_t c = g.at(i0, j);
+    const float4 pv = ld4(psrc + c);
+    if (first) return pv;
+    const float4 rv = ld4(q.r + c);
+    return make_float4(fmaf(beta, pv.x, rv.x), fmaf(beta, pv.y, rv.y), fmaf(beta, pv.z, rv.z),
+                       fmaf(beta, pv.w, rv.w));
+  }
+
+  __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
+    const int nx = g.nx, ny = g.ny;
+    const int lane = threadIdx.x & 31;
+    const bool valid = i0 < nx;
+    const int ncell = valid ? min(4, nx - i0) : 0;  // cells this lane owns
+    const float beta = (float)F.sc->beta;
+    const bool first = F.sc->first != 0;
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+
+    float4 pc = pn4(i0, j0, beta, first, valid);
+    float4 ps = (j0 > 0) ? pn4(i0, j0 - 1, beta, first, valid) : pc;
+    float4 kyc = valid ? ld4(q.ky + g.at(i0, j0)) : z;
+    for (int j = j0; j < j1; ++j) {
+      const float4 pnn = (j + 1 < ny) ? pn4(i0, j + 1, beta, first, valid) : pc;
+      const float4 kyn = valid ? ld4(q.ky + g.at(i0, j + 1)) : z;
+      const float4 kx4 = valid ? ld4(q.kx + g.at(i0, j)) : z;
+      float pw = __shfl_up_sync(FULL, pc.w, 1);
+      float pe = __shfl_down_sync(FULL, pc.x, 1);
+      float kxe = __shfl_down_sync(FULL, kx4.x, 1);
+      if (valid) {
+        if (i0 == 0) pw = pc.x;
+        else if (lane == 0) pw = pn1(i0 - 1, j, beta, first);
+        if (ncell == 4) {
+          if (i0 + 4 >= nx) {
+            pe = pc.w;                              // reflect at i = nx-1
+            kxe = __ldg(q.kx + g.at(i0 + 4, j));    // kx of the halo column
+          } else if (lane == 31) {
+            pe = pn1(i0 + 4, j, beta, first);
+            kxe = __ldg(q.kx + g.at(i0 + 4, j));
+          }
+        }
+        float wv[4];
+        double a = acc[0];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          if (k < ncell) {
+            const float c = comp(pc, k);
+            const float e = (k + 1 < ncell) ? comp(pc, k + 1) : (k == 3 ? pe : c);  // reflect past nx-1
+            const float wl = (k == 0) ? pw : comp(pc, k - 1);
+            const float k1 = (k == 3) ? kxe : comp(kx4, k + 1);
+            const float k0 = comp(kx4, k);
+            const float n = comp(pnn, k), s = comp(ps, k);
+            float t = c;
+            t = fmaf(k1, c - e, t);
+            t = fmaf(k0, c - wl, t);
+            t = fmaf(comp(kyn, k), c - n, t);
+            t = fmaf(comp(kyc, k), c - s, t);
+            wv[k] = t;
+            a = fma((double)t, (double)c, a);
+          } else {
+            wv[k] = 0.f;
+          }
+        }
+        acc[0] = a;
+        const size_t c0 = g.at(i0, j);
+        if (ncell == 4) {
+          st4(q.w + c0, make_float4(wv[0], wv[1], wv[2], wv[3]));
+          st4(pdst + c0, pc);
+        } else {
+          for (int k = 0; k < ncell; ++k) {
+            q.w[c0 + k] = wv[k];
+            pdst[c0 + k] = comp(pc, k);
+          }
+        }
+      }
+      ps = pc;
+      pc = pnn;
+      kyc = kyn;
+    }
+  }
+  __device__ void fin(const double *tot) const {
+    DevScalars *sc = F.sc;
+    sc->pw = tot[0];
+    sc->alpha = sc->rro / sc->pw;
+  }
+};
+
+// UR step: x += alpha p', r -= alpha w, r.r; the epilogue decides whether the
+// next step is another FP32 iteration or a refinement.
+struct OpIrUR {
+  static constexpr bool REDUCES = true;
+  Fields F;
+  G32 g;
+  IrPtrs q;
+  const float *__restrict__ p;
+  int guard;
+  cudaGraphConditionalHandle cond;
+  int set_cond;
+  __device__ bool skip() const { return guard && F.sc->done; }
+  __device__ void on_skip() const {
+    if (set_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0u);
+  }
+  __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
+    if (i0 >= g.nx) return;
+    const int ncell = min(4, g.nx - i0);
+    const float alpha = (float)F.sc->alpha;
+    double a = acc[0];
+    for (int j = j0; j < j1; ++j) {
+      const size_t c = g.at(i0, j);
+      if (ncell == 4) {
+        const float4 pv = ld4(p + c), wv = ld4(q.w + c);
+        float4 xv = ld4(q.x + c), rv = ld4(q.r + c);
+        xv.x = fmaf(alpha, pv.x, xv.x); xv.y = fmaf(alpha, pv.y, xv.y);
+        xv.z = fmaf(alpha, pv.z, xv.z); xv.w = fmaf(alpha, pv.w, xv.w);
+        rv.x = fmaf(-alpha, wv.x, rv.x); rv.y = fmaf(-alpha, wv.y, rv.y);
+        rv.z = fmaf(-alpha, wv.z, rv.z); rv.w = fmaf(-alpha, wv.w, rv.w);
+        a = fma((double)rv.x, (double)rv.x, a);
+        a = fma((double)rv.y, (double)rv.y, a);
+        a = fma((double)rv.z, (double)rv.z, a);
+        a = fma((double)rv.w, (double)rv.w, a);
+        st4(q.x + c, xv);
+        st4(q.r + c, rv);
+      } else {
+        for (int k = 0; k < ncell; ++k) {
+          const float xv = fmaf(alpha, p[c + k], q.x[c + k]);
+          const float rv = fmaf(-alpha, q.w[c + k], q.r[c + k]);
+          q.x[c + k] = xv;
+          q.r[c + k] = rv;
+          a = fma((double)rv, (double)rv, a);
+        }
+      }
+    }
+    acc[0] = a;
+  }
+  __device__ void fin(const double *tot) const {
+    DevScalars *sc = F.sc;
+    const double rrn = tot[0];
+    sc->beta = rrn / sc->rro;
+    sc->rro = rrn;
+    sc->error = rrn;
+    sc->iter += 1;
+    sc->first = 0;
+    const bool claim = sqrt(rrn / sc->bb) < sc->eps;
+    const bool refine = claim || rrn < sc->delta2 * sc->rr_ref;
+    sc->converged = 0;
+    sc->switched = refine;
+    const int done = refine || sc->iter >= sc->maxiters;
+    sc->done = done;
+    if (set_cond) cudaGraphSetConditional(cond, done ? 0u : 1u);
+  }
+};
+
+// Refinement: u += x, x = 0 on the interior.
+__global__ void k_ir_fold(Fields F, Geom g, G32 g32, float *x) {
+  const long long n = (long long)g.nx * g.ny;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(k % g.nx), j = (int)(k / g.nx);
+    const size_t c = g.at(i, j), c32 = g32.at(i, j);
+    F.u[c] = F.u[c] + (double)x[c32];
+    x[c32] = 0.f;
+  }
+}
+
+// Refinement: r = u0 - A u in FP64 (reference operation order, u's halo read
+// from memory), r32 = (float) r, sum r^2.
+struct OpIrResid : NoSkip {
+  Fields F;
+  Geom g;
+  G32 g32;
+  float *r32;
+  __device__ void cell(int i, int j, double (&acc)[1]) const {
+    const size_t c = g.at(i, j);
+    const double kxr = F.kx[c + 1], kxc = F.kx[c], kyt = F.ky[c + g.pitch], kyc = F.ky[c];
+    const double *a = F.u;
+    const double consum = tl::dadd(tl::dadd(tl::dadd(tl::dadd(1.0, kxr), kxc), kyt), kyc);
+    double v = tl::dmul(consum, a[c]);
+    v = tl::dsub(v, tl::dadd(tl::dmul(kxr, a[c + 1]), tl::dmul(kxc, a[c - 1])));
+    v = tl::dsub(v, tl::dadd(tl::dmul(kyt, a[c + g.pitch]), tl::dmul(kyc, a[c - g.pitch])));
+    const double t = tl::dsub(F.u0[c], v);
+    F.r[c] = t;
+    r32[g32.at(i, j)] = (float)t;
+    acc[0] = tl::dadd(acc[0], tl::dmul(t, t));
+  }
+  __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
+    for (int j = j0; j < j1; ++j) {
+      if (i0 < g.nx) cell(i0, j, acc);
+      if (i0 + 1 < g.nx) cell(i0 + 1, j, acc);
+    }
+  }
+  __device__ void fin(const double *tot) const { F.sc->red[0] = tot[0]; }
+};
+
+// FP32 copies of kx, ky (whole arrays, halo included); p32 = r32 = (float) r
+// and x = 0 on the interior.
+__global__ void k_ir_convert(Fields F, Geom g, G32 g32, float *kx, float *ky, float *r, float *p, float *x) {
+  const long long n = (long long)g.X * g.Y;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const int I = (int)(k % g.X), J = (int)(k / g.X);
+    const size_t c = (size_t)I + (size_t)J * g.pitch, c32 = (size_t)I + (size_t)J * g32.pitch;
+    kx[c32] = (float)F.kx[c];
+    ky[c32] = (float)F.ky[c];
+    const bool interior = I >= g.hd && I < g.X - g.hd && J >= g.hd && J < g.Y - g.hd;
+    const float rv = interior ? (float)F.r[c] : 0.f;
+    r[c32] = rv;
+    p[c32] = rv;
+    x[c32] = 0.f;
+  }
+}
+
+// p (FP64) = (double) p32 on the interior: the last search direction.
+__global__ void k_ir_export_p(Fields F, Geom g, G32 g32, const float *p32) {
+  const long long n = (long long)g.nx * g.ny;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(k % g.nx), j = (int)(k / g.nx);
+    F.p[g.at(i, j)] = (double)p32[g32.at(i, j)];
+  }
+}
+
+__global__ void k_ir_start(DevScalars *sc, double rr, double delta2) {
+  sc->rro = rr;
+  sc->rr_ref = rr;
+  sc->delta2 = delta2;
+  sc->done = 0;
+  sc->switched = 0;
+}
+
+int grid_for(long long n) {
+  long long b = (n + 255) / 256;
+  if (b > 152LL * 32) b = 152LL * 32;
+  return (int)(b < 1 ? 1 : b);
+}
+
+G32 g32_of(tl_ctx *ctx) {
+  G32 g;
+  g.nx = ctx->g.nx;
+  g.ny = ctx->g.ny;
+  g.hd = ctx->g.hd;
+  g.X = ctx->g.X;
+  g.Y = ctx->g.Y;
+  g.pitch = ctx->ir->pitch;
+  return g;
+}
+
+IrPtrs ptrs_of(tl_ctx *ctx) {
+  IrPtrs q;
+  q.kx = ctx->ir->kx;
+  q.ky = ctx->ir->ky;
+  q.r = ctx->ir->r;
+  q.w = ctx->ir->w;
+  q.x = ctx->ir->x;
+  return q;
+}
+
+void launch_ir_w(tl_ctx *ctx, const float *psrc, float *pdst, int guard) {
+  OpIrW op;
+  op.F = ctx->F;
+  op.g = g32_of(ctx);
+  op.q = ptrs_of(ctx);
+  op.psrc = psrc;
+  op.pdst = pdst;
+  op.guard = guard;
+  const Walk &wk = ctx->ir->walk;
+  k_walk32<OpIrW><<<wk.blocks, 32 * wk.warps, 0, ctx->stream>>>(op, wk, ctx->g.ny);
+}
+
+void launch_ir_ur(tl_ctx *ctx, const float *p, int guard, cudaGraphConditionalHandle cond, int set_cond) {
+  OpIrUR op;
+  op.F = ctx->F;
+  op.g = g32_of(ctx);
+  op.q = ptrs_of(ctx);
+  op.p = p;
+  op.guard = guard;
+  op.cond = cond;
+  op.set_cond = set_cond;
+  const Walk &wk = ctx->ir->walk;
+  k_walk32<OpIrUR><<<wk.blocks, 32 * wk.warps, 0, ctx->stream>>>(op, wk, ctx->g.ny);
+}
+
+int ensure_ir(tl_ctx *ctx) {
+  if (ctx->ir) return TL_OK;
+  tl_ir_state *ir = new (std::nothrow) tl_ir_state();
+  if (!ir) return TL_ERR_NOMEM;
+  ctx->ir = ir;
+  const Geom &g = ctx->g;
+  ir->pitch = (g.X + 31) / 32 * 32;
+  ir->lead = (32 - g.hd % 32) % 32;
+  ir->stride = (ir->lead + ir->pitch * (long long)g.Y + 64 + 63) / 64 * 64;
+  CK(cudaMalloc(&ir->buf, sizeof(float) * ir->stride * 7));
+  CK(cudaMemsetAsync(ir->buf, 0, sizeof(float) * ir->stride * 7, ctx->stream));
+  float *f[7];
+  for (int k = 0; k < 7; ++k) f[k] = ir->buf + ir->stride * k + ir->lead;
+  ir->kx = f[0]; ir->ky = f[1]; ir->p = f[2]; ir->pb = f[3]; ir->r = f[4]; ir->w = f[5]; ir->x = f[6];
+  Walk &w = ir->walk;
+  w.warps = 8;
+  w.rows = 32;
+  w.ntx = (g.nx + 128 * w.warps - 1) / (128 * w.warps);
+  w.tiles = w.ntx * ((g.ny + w.rows - 1) / w.rows);
+  const int cap = ctx->walk_fast.blocks > 0 ? ctx->walk_fast.blocks : 3 * ctx->sm_count;  // partials room
+  w.blocks = w.tiles < cap ? w.tiles : cap;
+  if (w.blocks < 1) w.blocks = 1;
+  return TL_OK;
+}
+
+int ir_graph(tl_ctx *ctx, int which, cudaGraphExec_t *out) {
+  tl_ir_state *ir = ctx->ir;
+  if (ir->graph[which]) {
+    *out = ir->graph[which];
+    return TL_OK;
+  }
+  cudaGraph_t graph = nullptr;
+  CK(cudaGraphCreate(&graph, 0));
+  cudaGraphConditionalHandle h;
+  cudaError_t e = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return tl_cuda_fail(ctx, e, "cudaGraphConditionalHandleCreate", __LINE__);
+  }
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return tl_cuda_fail(ctx, e, "cudaGraphAddNode(while)", __LINE__);
+  }
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  e = cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return tl_cuda_fail(ctx, e, "cudaStreamBeginCaptureToGraph", __LINE__);
+  }
+  float *a = which ? ir->pb : ir->p, *b = which ? ir->p : ir->pb;
+  launch_ir_w(ctx, a, b, 0);
+  launch_ir_ur(ctx, b, 0, h, 0);
+  launch_ir_w(ctx, b, a, 1);
+  launch_ir_ur(ctx, a, 1, h, 1);
+  cudaError_t le = cudaGetLastError();
+  cudaGraph_t captured = nullptr;
+  e = cudaStreamEndCapture(ctx->stream, &captured);
+  if (e != cudaSuccess || le != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return tl_cuda_fail(ctx, e != cudaSuccess ? e : le, "capture of the FP32 loop", __LINE__);
+  }
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return tl_cuda_fail(ctx, e, "cudaGraphInstantiate", __LINE__);
+  ir->graph[which] = exec;
+  *out = exec;
+  return TL_OK;
+}
+
+}  // namespace
+
+void tl_release_ir(tl_ctx *ctx) {
+  if (!ctx->ir) return;
+  for (auto &gx : ctx->ir->graph)
+    if (gx) cudaGraphExecDestroy(gx);
+  if (ctx->ir->buf) cudaFree(ctx->ir->buf);
+  delete ctx->ir;
+  ctx->ir = nullptr;
+}
+
+// The refinement step.  Returns the true r.r in *rr.
+static int refine(tl_ctx *ctx, double *rr) {
+  const G32 g32 = g32_of(ctx);
+  k_ir_fold<<<grid_for((long long)ctx->g.nx * ctx->g.ny), 256, 0, ctx->stream>>>(ctx->F, ctx->g, g32, ctx->ir->x);
+  CKL();
+  double *u = ctx->F.u;
+  launch_halo(ctx->stream, &u, 1, ctx->g, 1, TL_MODE_TEALEAF);
+  CKL();
+  OpIrResid op;
+  op.F = ctx->F;
+  op.g = ctx->g;
+  op.g32 = g32;
+  op.r32 = ctx->ir->r;
+  launch_walk<1>(ctx->stream, op, ctx->walk_exact, ctx->g.ny);
+  CKL();
+  ctx->launches += 3;
+  int rc = tl_read_scalars(ctx);
+  if (rc) return rc;
+  *rr = ctx->host_sc->red[0];
+  return TL_OK;
+}
+
+int tl_ir_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res) {
+  if (ctx->cfg.mode != TL_MODE_TEALEAF) {
+    tl_set_error(ctx, "FP32 refinement needs the tealeaf (5-point) semantics");
+    return TL_ERR_ARG;
+  }
+  int rc = ensure_ir(ctx);
+  if (rc) return rc;
+  tl_params p = *prm;
+  p.criterion = TL_CRIT_RELATIVE;
+  if ((rc = tl_cg_init(ctx, rx, ry, p.coefficient, 1))) return rc;
+  if ((rc = tl_set_loop_params(ctx, &p, 0, 0))) return rc;
+  const int up[2] = {TL_EX_U, TL_EX_P};
+  if ((rc = tl_halo_update(ctx, 1, up, 2, 1))) return rc;
+  if ((rc = tl_copy_u(ctx))) return rc;
+  const G32 g32 = g32_of(ctx);
+  tl_ir_state *ir = ctx->ir;
+  k_ir_convert<<<grid_for((long long)ctx->g.X * ctx->g.Y), 256, 0, ctx->stream>>>(ctx->F, ctx->g, g32, ir->kx, ir->ky,
+                                                                                  ir->r, ir->p, ir->x);
+  CKL();
+  ctx->launches += 8;
+  if ((rc = tl_read_scalars(ctx))) return rc;
+  const double bb = ctx->host_sc->bb;
+  double rr = ctx->host_sc->rro;
+  double rel = bb > 0 ? sqrt(rr / bb) : sqrt(rr);
+  int which = 0, refinements = 0;
+  ctx->last_solve_ms = 0.0;
+  while (rel >= p.eps && ctx->host_sc->iter < p.maxiters) {
+    k_ir_start<<<1, 1, 0, ctx->stream>>>(ctx->F.sc, rr, IR_DELTA * IR_DELTA);
+    CKL();
+    cudaGraphExec_t exec;
+    if ((rc = ir_graph(ctx, which, &exec))) return rc;
+    const int before = ctx->host_sc->iter;
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    CK(cudaGraphLaunch(exec, ctx->stream));
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    CK(cudaEventSynchronize(ctx->ev1));
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1));
+    ctx->last_solve_ms += t;
+    if ((rc = tl_read_scalars(ctx))) return rc;
+    const int trips = ctx->host_sc->iter - before;
+    ctx->launches += 1 + 4LL * ((trips + 1) / 2);
+    if (trips & 1) which ^= 1;  // the last step wrote p into the other buffer
+    if ((rc = refine(ctx, &rr))) return rc;
+    ++refinements;
+    rel = bb > 0 ? sqrt(rr / bb) : sqrt(rr);
+  }
+  float *pcur = which ? ir->pb : ir->p;
+  k_ir_export_p<<<grid_for((long long)ctx->g.nx * ctx->g.ny), 256, 0, ctx->stream>>>(ctx->F, ctx->g, g32, pcur);
+  CKL();
+  if ((rc = tl_halo_update(ctx, 1, up, 2, 1))) return rc;
+  ctx->launches += 2;
+  if ((rc = tl_read_scalars(ctx))) return rc;
+  res->iters = ctx->host_sc->iter;
+  res->cg_iters = ctx->host_sc->iter;
+  res->error = rr;
+  res->rel_residual = rel;
+  res->converged = rel < p.eps;
+  res->refinements = refinements;
+  res->launches = (int)ctx->launches;
+  return TL_OK;
+}
+
+int tl_ir_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch) {
+  int rc = ensure_ir(ctx);
+  if (rc) return rc;
+  if (kernel != 2 && kernel != 3) return TL_ERR_ARG;
+  tl_ir_state *ir = ctx->ir;
+  CK(cudaEventRecord(ctx->tev0, ctx->stream));
+  for (int k = 0; k < reps; ++k) {
+    if (kernel == 2) launch_ir_w(ctx, (k & 1) ? ir->pb : ir->p, (k & 1) ? ir->p : ir->pb, 0);
+    else launch_ir_ur(ctx, ir->pb, 0, 0, 0);
+  }
+  CKL();
+  CK(cudaEventRecord(ctx->tev1, ctx->stream));
+  CK(cudaEventSynchronize(ctx->tev1));
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, ctx->tev0, ctx->tev1));
+  *ms_per_launch = t / reps;
+  return TL_OK;
 }
