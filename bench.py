@@ -179,8 +179,9 @@ def run_variant(tl, n, precision, steps, warmup):
 
 
 def run_e2e(tl, n, precision, steps, warmup):
-    """The same timestep through the C ABI with host buffers: upload energy and
-    density from pinned memory, solve, solvefinished, download energy."""
+    """The same timesteps through the C ABI with host buffers: each step uploads
+    energy and density from pinned memory, solves, runs solvefinished and
+    downloads energy; the W warm-up steps go through the same path untimed."""
     import torch
     s, chunk = gpu_setup(tl, n, precision)
     lib = chunk.lib
@@ -188,41 +189,41 @@ def run_e2e(tl, n, precision, steps, warmup):
     pinned = {nm: torch.empty((Y, X), dtype=torch.float64, pin_memory=True) for nm in ("energy", "density")}
     out = torch.empty((Y, X), dtype=torch.float64, pin_memory=True)
     for nm in pinned:
-        a = chunk.field(nm)
-        pinned[nm].numpy()[...] = a.T
-    fidx = {nm: ["density0", "density", "energy0", "energy", "u", "u0", "p", "r", "mi", "w", "kx", "ky", "sd",
-                 "volume"].index(nm) for nm in ("energy", "density")}
+        pinned[nm].numpy()[...] = chunk.field(nm).T
+    fidx = {"energy": 3, "density": 1}
     dptr = C.POINTER(C.c_double)
-    times, h2d, d2h = [], 0, 0
+    times = []
     for k in range(warmup + steps):
         chunk.check(lib.tl_synchronize(chunk.ctx))
         chunk.check(lib.tl_timer_start(chunk.ctx))
         for nm in ("energy", "density"):
             chunk.check(lib.tl_upload(chunk.ctx, fidx[nm], C.cast(pinned[nm].data_ptr(), dptr), X))
-        r = timestep(tl, chunk, s)
+        timestep(tl, chunk, s)
         chunk.check(lib.tl_download(chunk.ctx, fidx["energy"], C.cast(out.data_ptr(), dptr), X))
         ms = C.c_double()
         chunk.check(lib.tl_timer_stop(chunk.ctx, C.byref(ms)))
-        # the next step starts from this step's result, as diffuse! does
-        pinned["energy"].copy_(out)
+        pinned["energy"].copy_(out)     # the next step starts from this step's result, as diffuse! does
         if k >= warmup:
             times.append(ms.value)
-            h2d = 2 * X * Y * 8
-            d2h = X * Y * 8
     chunk.close()
-    return statistics.mean(times), h2d, d2h
+    return statistics.mean(times), 2 * X * Y * 8, X * Y * 8
 
 
-def kernel_roofline(tl, chunk, peaks):
-    """Average duration of the dominant fused kernels, timed alone with events."""
+KERNELS = {"fp64": ((0, "cg_w_step", W_STEP_BYTES), (1, "cg_ur_step", UR_STEP_BYTES)),
+           "fp32_ir": ((2, "ir_w_step", 24), (3, "ir_ur_step", 24))}
+
+
+def kernel_roofline(tl, chunk, variant):
+    """Average duration of the variant's two iteration kernels, each launched
+    20 times back to back on the library's stream and timed with CUDA events;
+    algorithmic bytes = compulsory reads + writes per interior cell."""
     lib = chunk.lib
     cells = chunk.settings.xcells * chunk.settings.ycells
     out = {}
-    for k, name, b in ((0, "cg_w_step", W_STEP_BYTES), (1, "cg_ur_step", UR_STEP_BYTES)):
+    for k, name, b in KERNELS[variant]:
         ms = C.c_double()
         chunk.check(lib.tl_bench_kernel(chunk.ctx, k, 20, C.byref(ms)))
-        gbs = b * cells / (ms.value * 1e-3) / 1e9
-        out[name] = {"ms": ms.value, "bytes_per_cell": b, "gbs": gbs}
+        out[name] = {"ms": ms.value, "bytes_per_cell": b, "gbs": b * cells / (ms.value * 1e-3) / 1e9}
     return out
 
 
@@ -327,8 +328,9 @@ def gpu_arm(args):
             variants[name] = {"ms_per_step": mean_ms, "max_ms": ms, "iters": iters,
                               "rel_residual": [r.rel_residual for r in results],
                               "loop_ms": loop_ms, "launches": [r.launches for r in results],
-                              "gbs_per_iteration": BYTES_PER_CELL_ITER * n * n * statistics.mean(iters) /
-                              (statistics.mean(loop_ms) * 1e-3) / 1e9 if name == "fp64" else None}
+                              "ms_per_iteration": statistics.mean(loop_ms) / statistics.mean(iters),
+                              "algorithmic_gbs_per_iteration": (BYTES_PER_CELL_ITER if name == "fp64" else 48) *
+                              n * n * statistics.mean(iters) / (statistics.mean(loop_ms) * 1e-3) / 1e9}
             if headline is None:
                 headline = (name, chunk, results)
             else:
@@ -338,9 +340,9 @@ def gpu_arm(args):
         print(json.dumps({"metric": METRIC, "error": variants}))
         return
     hname, hchunk, hres = headline
-    roof = kernel_roofline(tl, hchunk, peak) if hname == "fp64" else None
+    roof = kernel_roofline(tl, hchunk, hname)
     hchunk.close()
-    e2e_ms, h2d, d2h = run_e2e(tl, n, prec[hname], max(1, min(args.steps, 2)), 1)
+    e2e_ms, h2d, d2h = run_e2e(tl, n, prec[hname], args.steps, args.warmup)
     value = variants[hname]["ms_per_step"]
     line = {"metric": METRIC, "value": value, "unit": "ms", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False, "scaling": "weak",
@@ -351,7 +353,8 @@ def gpu_arm(args):
                        "variant": hname, "l2": "every field (537 MB at 8192^2) is larger than L2; no flush"},
             "clocks": clocks,
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "gpu_launches": int(sum(r.launches for r in hres) + 6 * len(hres)),
+            # the solve's own launches plus the halo and solvefinished! kernels of each step
+            "gpu_launches": int(sum(r.launches for r in hres) + 4 * len(hres)),
             "variants": variants}
     if roof:
         dom = max(roof.values(), key=lambda d: d["ms"])

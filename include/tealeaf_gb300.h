@@ -153,6 +153,13 @@ int tl_get_cg_coefficients(tl_ctx *ctx, double *alpha, double *beta, int n);
  * per tile, persistent blocks.  Lets a checker reproduce the summation order. */
 int tl_reduction_layout(tl_ctx *ctx, int *warps, int *rows, int *blocks);
 
+/* Launch layout (warps per block, rows per tile, persistent blocks) of one
+ * fused iteration kernel (ids as in tl_bench_kernel): get the autotuned
+ * choice, or override it (both for tuning studies; a set layout holds until
+ * the context is destroyed). */
+int tl_get_layout(tl_ctx *ctx, int kernel, int *warps, int *rows, int *blocks);
+int tl_set_layout(tl_ctx *ctx, int kernel, int warps, int rows, int blocks);
+
 /* Wait for all work queued on the context. */
 int tl_synchronize(tl_ctx *ctx);
 

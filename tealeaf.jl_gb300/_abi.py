@@ -67,6 +67,8 @@ SIGNATURES = {
     "tl_get_cg_coefficients": ([_CTX, _P(C.c_double), _P(C.c_double), C.c_int], C.c_int),
     "tl_reduction_layout": ([_CTX, _P(C.c_int), _P(C.c_int), _P(C.c_int)], C.c_int),
     "tl_synchronize": ([_CTX], C.c_int),
+    "tl_get_layout": ([_CTX, C.c_int, _P(C.c_int), _P(C.c_int), _P(C.c_int)], C.c_int),
+    "tl_set_layout": ([_CTX, C.c_int, C.c_int, C.c_int, C.c_int], C.c_int),
     "tl_last_solve_ms": ([_CTX, _P(C.c_double)], C.c_int),
     "tl_timer_start": ([_CTX], C.c_int),
     "tl_timer_stop": ([_CTX, _P(C.c_double)], C.c_int),

@@ -88,8 +88,10 @@ extern "C" int tl_create(tl_ctx **out, const tl_config *cfg) {
   CK(cudaEventCreate(&ctx->tev1));
 
   ctx->walk_exact = make_walk(g.nx, g.ny, EXACT_WARPS, EXACT_ROWS, 2 * ctx->sm_count);
-  ctx->walk_fast = tl_tune_walk(ctx);
-  const int max_blocks = ctx->walk_exact.blocks > ctx->walk_fast.blocks ? ctx->walk_exact.blocks : ctx->walk_fast.blocks;
+  ctx->max_blocks = 8 * ctx->sm_count;  // the autotuner tries at most 8 resident blocks per SM
+  const int max_blocks = ctx->max_blocks;
+  const char *loop = getenv("TEALEAF_GB300_LOOP");
+  ctx->host_loop = loop && !strcmp(loop, "host");
 
   // fields: TL_NFIELDS reference fields + pb, ub, sdb, diag
   const int nbuf = TL_NFIELDS + 4;
@@ -97,6 +99,7 @@ extern "C" int tl_create(tl_ctx **out, const tl_config *cfg) {
   ctx->field_stride = per;
   CK(cudaMalloc(&ctx->buf, sizeof(double) * per * nbuf));
   CK(cudaMemsetAsync(ctx->buf, 0, sizeof(double) * per * nbuf, ctx->stream));
+  ctx->buf_bytes = sizeof(double) * per * nbuf;
   double *f[nbuf];
   for (int k = 0; k < nbuf; ++k) f[k] = ctx->buf + per * k + ctx->lead;
   Fields &F = ctx->F;
@@ -116,10 +119,20 @@ extern "C" int tl_create(tl_ctx **out, const tl_config *cfg) {
   F.partials = F.chebybeta + tab;
   F.sc = reinterpret_cast<DevScalars *>(F.partials + (size_t)MAX_RED * max_blocks);
   F.counter = reinterpret_cast<unsigned *>(reinterpret_cast<char *>(F.sc) + sizeof(DevScalars));
-  CK(cudaMemsetAsync(ctx->small, 0, sizeof(double) * (4 * tab + (size_t)MAX_RED * max_blocks) + sizeof(DevScalars) + 256,
-                     ctx->stream));
+  ctx->small_bytes = sizeof(double) * (4 * tab + (size_t)MAX_RED * max_blocks) + sizeof(DevScalars) + 256;
+  CK(cudaMemsetAsync(ctx->small, 0, ctx->small_bytes, ctx->stream));
   CK(cudaMallocHost(&ctx->host_sc, sizeof(DevScalars)));
 
+  if (cfg->mode == TL_MODE_TEALEAF) {
+    // Tune the fused kernels on the zeroed fields, then zero everything the
+    // trial launches touched (they leave NaN behind: alpha = 0/0).
+    ctx->walk_w64 = tl_autotune(ctx, 64, tl_occupancy_cg(0, 128), tl_occupancy_cg(0, 256), tl_launch_w64_for_tuning);
+    ctx->walk_ur64 = tl_autotune(ctx, 64, tl_occupancy_cg(1, 128), tl_occupancy_cg(1, 256), tl_launch_ur64_for_tuning);
+    CK(cudaMemsetAsync(ctx->buf, 0, ctx->buf_bytes, ctx->stream));
+    CK(cudaMemsetAsync(ctx->small, 0, ctx->small_bytes, ctx->stream));
+  } else {
+    ctx->walk_w64 = ctx->walk_ur64 = ctx->walk_exact;
+  }
   launch_fill(ctx->stream, F.volume, g, cfg->dx * cfg->dy);  // chunk.jl:79
   CKL();
   CK(cudaStreamSynchronize(ctx->stream));
@@ -371,15 +384,14 @@ extern "C" int tl_timer_stop(tl_ctx *ctx, double *ms) {
 extern "C" int tl_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch) {
   if (!ctx || !ms_per_launch || reps < 1 || ctx->cfg.mode != TL_MODE_TEALEAF) return TL_ERR_ARG;
   const Fields &F = ctx->F;
-  const Walk &wk = ctx->walk_fast;
   if (kernel >= 2) return tl_ir_bench_kernel(ctx, kernel, reps, ms_per_launch);
   if (kernel < 0) return TL_ERR_ARG;
   launch_init_diag(ctx->stream, F, ctx->g);
   CKL();
   CK(cudaEventRecord(ctx->tev0, ctx->stream));
   for (int k = 0; k < reps; ++k) {
-    if (kernel == 0) launch_tl_w(ctx->stream, F, ctx->g, wk, (k & 1) ? F.pb : F.p, (k & 1) ? F.p : F.pb, 0, 0);
-    else launch_tl_ur(ctx->stream, F, ctx->g, wk, F.pb, 0, 0, 0, 0);
+    if (kernel == 0) launch_tl_w(ctx->stream, F, ctx->g, ctx->walk_w64, (k & 1) ? F.pb : F.p, (k & 1) ? F.p : F.pb, 0, 0);
+    else launch_tl_ur(ctx->stream, F, ctx->g, ctx->walk_ur64, F.pb, 0, 0, 0, 0);
   }
   CKL();
   CK(cudaEventRecord(ctx->tev1, ctx->stream));
@@ -387,5 +399,52 @@ extern "C" int tl_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per
   float t = 0.f;
   CK(cudaEventElapsedTime(&t, ctx->tev0, ctx->tev1));
   *ms_per_launch = t / reps;
+  return TL_OK;
+}
+
+static Walk *layout_of(tl_ctx *ctx, int kernel) {
+  if (ctx->cfg.mode != TL_MODE_TEALEAF) return nullptr;
+  switch (kernel) {
+    case 0: return &ctx->walk_w64;
+    case 1: return &ctx->walk_ur64;
+    case 2:
+    case 3: return tl_ir_walk(ctx, kernel);
+    default: return nullptr;
+  }
+}
+
+extern "C" int tl_get_layout(tl_ctx *ctx, int kernel, int *warps, int *rows, int *blocks) {
+  if (!ctx) return TL_ERR_ARG;
+  Walk *w = layout_of(ctx, kernel);
+  if (!w) {
+    tl_set_error(ctx, "no tuned layout for kernel %d in this mode", kernel);
+    return TL_ERR_ARG;
+  }
+  if (warps) *warps = w->warps;
+  if (rows) *rows = w->rows;
+  if (blocks) *blocks = w->blocks;
+  return TL_OK;
+}
+
+extern "C" int tl_set_layout(tl_ctx *ctx, int kernel, int warps, int rows, int blocks) {
+  if (!ctx) return TL_ERR_ARG;
+  Walk *w = layout_of(ctx, kernel);
+  if (!w || (warps != 4 && warps != 8) || rows < 1 || blocks < 1 || blocks > ctx->max_blocks) {
+    tl_set_error(ctx, "invalid layout for kernel %d: %d warps, %d rows, %d blocks (at most %d)", kernel, warps, rows,
+                 blocks, ctx->max_blocks);
+    return TL_ERR_ARG;
+  }
+  const int cols = kernel >= 2 ? 128 : 64;
+  const int TW = cols * warps;
+  Walk n;
+  n.warps = warps;
+  n.rows = rows;
+  n.ntx = (ctx->g.nx + TW - 1) / TW;
+  n.tiles = n.ntx * ((ctx->g.ny + rows - 1) / rows);
+  n.blocks = blocks < n.tiles ? blocks : n.tiles;
+  *w = n;
+  // graphs hold the old launch configuration
+  tl_release_graphs(ctx);
+  tl_release_ir_graphs(ctx);
   return TL_OK;
 }

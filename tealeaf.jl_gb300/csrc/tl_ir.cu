@@ -1,8 +1,9 @@
 // tl_ir.cu -- CG with FP32 inner sweeps inside FP64 refinement.
 //
 // The inner iteration is CG on FP32 vectors (p, r, w and the correction x)
-// with FP32 Kx/Ky; its dots multiply the FP32 operands exactly in FP64 and
-// accumulate in FP64.  Whenever the FP32 residual has dropped by a factor
+// with FP32 Kx/Ky; each dot sums a lane's four products in FP32 and
+// accumulates those partial sums in FP64 (one FP64 add per four cells: the
+// FP64 pipe of this part issues 1/64 as fast as FP32).  Whenever the FP32 residual has dropped by a factor
 // delta since the last refinement, or claims convergence, the loop returns to
 // a refinement step done entirely in FP64:
 //     u += x;  x = 0;  r = u0 - A u (true residual);  test ||r|| / ||u0||.
@@ -28,7 +29,7 @@ struct tl_ir_state {
   float *buf = nullptr;
   long long pitch = 0, lead = 0, stride = 0;
   float *kx = nullptr, *ky = nullptr, *p = nullptr, *pb = nullptr, *r = nullptr, *w = nullptr, *x = nullptr;
-  Walk walk{};
+  Walk walk_w{}, walk_ur{};  // autotuned layouts of the two FP32 kernels
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // p in the first / second buffer
 };
 
@@ -84,19 +85,27 @@ struct OpIrW {
   __device__ bool skip() const { return guard && F.sc->done; }
   __device__ void on_skip() const {}
 
-  __device__ __forceinline__ float pn1(int i, int j, float beta, bool first) const {
-    const size_t c = g.at(i, j);
-    const float pv = __ldg(psrc + c);
-    return first ? pv : fmaf(beta, pv, __ldg(q.r + c));
-  }
-  __device__ __forceinline__ float4 pn4(int i0, int j, float beta, bool first, bool valid) const {
-    if (!valid) return make_float4(0.f, 0.f, 0.f, 0.f);
+  // Raw loads of one row, issued one row ahead of their use.
+  struct Row {
+    float4 p, r, kx;
+    float ep, er, kxe;  // edge neighbour (lane 0: i0-1, lane 31: i0+4) and kx at i0+4
+  };
+  __device__ __forceinline__ void load_row(Row &o, int i0, int j, bool valid, bool first, int edge_col) const {
+    if (!valid) return;
     const size_t c = g.at(i0, j);
-    const float4 pv = ld4(psrc + c);
-    if (first) return pv;
-    const float4 rv = ld4(q.r + c);
-    return make_float4(fmaf(beta, pv.x, rv.x), fmaf(beta, pv.y, rv.y), fmaf(beta, pv.z, rv.z),
-                       fmaf(beta, pv.w, rv.w));
+    o.p = ld4(psrc + c);
+    if (!first) o.r = ld4(q.r + c);
+    if (edge_col >= 0) {
+      const size_t e = g.at(edge_col, j);
+      o.ep = __ldg(psrc + e);
+      if (!first) o.er = __ldg(q.r + e);
+    }
+  }
+  __device__ __forceinline__ void load_coef(Row &o, int i0, int j, bool valid, bool kx_edge) const {
+    if (!valid) return;
+    const size_t c = g.at(i0, j);
+    o.kx = ld4(q.kx + c);
+    if (kx_edge) o.kxe = __ldg(q.kx + c + 4);
   }
 
   __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
@@ -104,57 +113,78 @@ struct OpIrW {
     const int lane = threadIdx.x & 31;
     const bool valid = i0 < nx;
     const int ncell = valid ? min(4, nx - i0) : 0;  // cells this lane owns
+    const bool full = ncell == 4;
+    const bool inner = i0 + 4 < nx;                 // the fourth cell has an interior east neighbour
     const float beta = (float)F.sc->beta;
     const bool first = F.sc->first != 0;
     const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int edge_col = !valid ? -1 : (lane == 0 && i0 > 0) ? i0 - 1 : (lane == 31 && inner) ? i0 + 4 : -1;
+    const bool kx_edge = full && (!inner || lane == 31);
+    auto pnew = [&](const Row &o) {
+      return first ? o.p
+                   : make_float4(fmaf(beta, o.p.x, o.r.x), fmaf(beta, o.p.y, o.r.y), fmaf(beta, o.p.z, o.r.z),
+                                 fmaf(beta, o.p.w, o.r.w));
+    };
+    auto pnew_edge = [&](const Row &o) { return first ? o.ep : fmaf(beta, o.ep, o.er); };
 
-    float4 pc = pn4(i0, j0, beta, first, valid);
-    float4 ps = (j0 > 0) ? pn4(i0, j0 - 1, beta, first, valid) : pc;
+    Row cur = {}, nxt = {}, tmp = {};
+    load_row(cur, i0, j0, valid, first, edge_col);
+    load_coef(cur, i0, j0, valid, kx_edge);
+    if (j0 > 0) load_row(tmp, i0, j0 - 1, valid, first, -1);
+    if (j0 + 1 < ny) load_row(nxt, i0, j0 + 1, valid, first, edge_col);
     float4 kyc = valid ? ld4(q.ky + g.at(i0, j0)) : z;
+    float4 kyn = valid ? ld4(q.ky + g.at(i0, j0 + 1)) : z;
+    float4 pc = valid ? pnew(cur) : z;
+    float4 ps = (j0 > 0 && valid) ? pnew(tmp) : pc;
     for (int j = j0; j < j1; ++j) {
-      const float4 pnn = (j + 1 < ny) ? pn4(i0, j + 1, beta, first, valid) : pc;
-      const float4 kyn = valid ? ld4(q.ky + g.at(i0, j + 1)) : z;
-      const float4 kx4 = valid ? ld4(q.kx + g.at(i0, j)) : z;
+      Row nn = {};
+      float4 kyn2 = z;
+      if (j + 1 < j1) {
+        if (j + 2 < ny) load_row(nn, i0, j + 2, valid, first, edge_col);
+        load_coef(nxt, i0, j + 1, valid, kx_edge);
+        kyn2 = valid ? ld4(q.ky + g.at(i0, j + 2)) : z;
+      }
+      const float4 pnn = (j + 1 < ny && valid) ? pnew(nxt) : pc;
       float pw = __shfl_up_sync(FULL, pc.w, 1);
       float pe = __shfl_down_sync(FULL, pc.x, 1);
-      float kxe = __shfl_down_sync(FULL, kx4.x, 1);
+      float kxe = __shfl_down_sync(FULL, cur.kx.x, 1);
       if (valid) {
         if (i0 == 0) pw = pc.x;
-        else if (lane == 0) pw = pn1(i0 - 1, j, beta, first);
-        if (ncell == 4) {
-          if (i0 + 4 >= nx) {
-            pe = pc.w;                              // reflect at i = nx-1
-            kxe = __ldg(q.kx + g.at(i0 + 4, j));    // kx of the halo column
+        else if (lane == 0) pw = pnew_edge(cur);
+        if (full) {
+          if (!inner) {
+            pe = pc.w;        // reflect at i = nx-1
+            kxe = cur.kxe;    // kx of the halo column
           } else if (lane == 31) {
-            pe = pn1(i0 + 4, j, beta, first);
-            kxe = __ldg(q.kx + g.at(i0 + 4, j));
+            pe = pnew_edge(cur);
+            kxe = cur.kxe;
           }
         }
         float wv[4];
-        double a = acc[0];
+        float part = 0.f;  // this lane's four products, summed in FP32 before the FP64 accumulation
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           if (k < ncell) {
             const float c = comp(pc, k);
             const float e = (k + 1 < ncell) ? comp(pc, k + 1) : (k == 3 ? pe : c);  // reflect past nx-1
             const float wl = (k == 0) ? pw : comp(pc, k - 1);
-            const float k1 = (k == 3) ? kxe : comp(kx4, k + 1);
-            const float k0 = comp(kx4, k);
-            const float n = comp(pnn, k), s = comp(ps, k);
+            const float k1 = (k == 3) ? kxe : comp(cur.kx, k + 1);
+            const float k0 = comp(cur.kx, k);
+            const float n = comp(pnn, k), sv = comp(ps, k);
             float t = c;
             t = fmaf(k1, c - e, t);
             t = fmaf(k0, c - wl, t);
             t = fmaf(comp(kyn, k), c - n, t);
-            t = fmaf(comp(kyc, k), c - s, t);
+            t = fmaf(comp(kyc, k), c - sv, t);
             wv[k] = t;
-            a = fma((double)t, (double)c, a);
+            part = fmaf(t, c, part);
           } else {
             wv[k] = 0.f;
           }
         }
-        acc[0] = a;
+        acc[0] += (double)part;
         const size_t c0 = g.at(i0, j);
-        if (ncell == 4) {
+        if (full) {
           st4(q.w + c0, make_float4(wv[0], wv[1], wv[2], wv[3]));
           st4(pdst + c0, pc);
         } else {
@@ -167,6 +197,9 @@ struct OpIrW {
       ps = pc;
       pc = pnn;
       kyc = kyn;
+      kyn = kyn2;
+      cur = nxt;
+      nxt = nn;
     }
   }
   __device__ void fin(const double *tot) const {
@@ -205,10 +238,7 @@ struct OpIrUR {
         xv.z = fmaf(alpha, pv.z, xv.z); xv.w = fmaf(alpha, pv.w, xv.w);
         rv.x = fmaf(-alpha, wv.x, rv.x); rv.y = fmaf(-alpha, wv.y, rv.y);
         rv.z = fmaf(-alpha, wv.z, rv.z); rv.w = fmaf(-alpha, wv.w, rv.w);
-        a = fma((double)rv.x, (double)rv.x, a);
-        a = fma((double)rv.y, (double)rv.y, a);
-        a = fma((double)rv.z, (double)rv.z, a);
-        a = fma((double)rv.w, (double)rv.w, a);
+        a += (double)fmaf(rv.w, rv.w, fmaf(rv.z, rv.z, fmaf(rv.y, rv.y, rv.x * rv.x)));
         st4(q.x + c, xv);
         st4(q.r + c, rv);
       } else {
@@ -342,7 +372,7 @@ IrPtrs ptrs_of(tl_ctx *ctx) {
   return q;
 }
 
-void launch_ir_w(tl_ctx *ctx, const float *psrc, float *pdst, int guard) {
+void launch_ir_w(tl_ctx *ctx, const float *psrc, float *pdst, int guard, const Walk *walk = nullptr) {
   OpIrW op;
   op.F = ctx->F;
   op.g = g32_of(ctx);
@@ -350,11 +380,12 @@ void launch_ir_w(tl_ctx *ctx, const float *psrc, float *pdst, int guard) {
   op.psrc = psrc;
   op.pdst = pdst;
   op.guard = guard;
-  const Walk &wk = ctx->ir->walk;
+  const Walk &wk = walk ? *walk : ctx->ir->walk_w;
   k_walk32<OpIrW><<<wk.blocks, 32 * wk.warps, 0, ctx->stream>>>(op, wk, ctx->g.ny);
 }
 
-void launch_ir_ur(tl_ctx *ctx, const float *p, int guard, cudaGraphConditionalHandle cond, int set_cond) {
+void launch_ir_ur(tl_ctx *ctx, const float *p, int guard, cudaGraphConditionalHandle cond, int set_cond,
+                  const Walk *walk = nullptr) {
   OpIrUR op;
   op.F = ctx->F;
   op.g = g32_of(ctx);
@@ -363,9 +394,19 @@ void launch_ir_ur(tl_ctx *ctx, const float *p, int guard, cudaGraphConditionalHa
   op.guard = guard;
   op.cond = cond;
   op.set_cond = set_cond;
-  const Walk &wk = ctx->ir->walk;
+  const Walk &wk = walk ? *walk : ctx->ir->walk_ur;
   k_walk32<OpIrUR><<<wk.blocks, 32 * wk.warps, 0, ctx->stream>>>(op, wk, ctx->g.ny);
 }
+
+int occupancy32(int kernel, int threads) {
+  int n = 0;
+  cudaError_t e = kernel == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_walk32<OpIrW>, threads, 0)
+                              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_walk32<OpIrUR>, threads, 0);
+  return e == cudaSuccess ? n : 1;
+}
+
+void tune_w32(tl_ctx *ctx, const Walk &wk) { launch_ir_w(ctx, ctx->ir->p, ctx->ir->pb, 0, &wk); }
+void tune_ur32(tl_ctx *ctx, const Walk &wk) { launch_ir_ur(ctx, ctx->ir->pb, 0, 0, 0, &wk); }
 
 int ensure_ir(tl_ctx *ctx) {
   if (ctx->ir) return TL_OK;
@@ -381,14 +422,11 @@ int ensure_ir(tl_ctx *ctx) {
   float *f[7];
   for (int k = 0; k < 7; ++k) f[k] = ir->buf + ir->stride * k + ir->lead;
   ir->kx = f[0]; ir->ky = f[1]; ir->p = f[2]; ir->pb = f[3]; ir->r = f[4]; ir->w = f[5]; ir->x = f[6];
-  Walk &w = ir->walk;
-  w.warps = 8;
-  w.rows = 32;
-  w.ntx = (g.nx + 128 * w.warps - 1) / (128 * w.warps);
-  w.tiles = w.ntx * ((g.ny + w.rows - 1) / w.rows);
-  const int cap = ctx->walk_fast.blocks > 0 ? ctx->walk_fast.blocks : 3 * ctx->sm_count;  // partials room
-  w.blocks = w.tiles < cap ? w.tiles : cap;
-  if (w.blocks < 1) w.blocks = 1;
+  // tune on the zeroed buffers, then zero them again: the trial launches
+  // leave NaN behind (alpha = 0/0)
+  ir->walk_w = tl_autotune(ctx, 128, occupancy32(0, 128), occupancy32(0, 256), tune_w32);
+  ir->walk_ur = tl_autotune(ctx, 128, occupancy32(1, 128), occupancy32(1, 256), tune_ur32);
+  CK(cudaMemsetAsync(ir->buf, 0, sizeof(float) * ir->stride * 7, ctx->stream));
   return TL_OK;
 }
 
@@ -445,6 +483,15 @@ int ir_graph(tl_ctx *ctx, int which, cudaGraphExec_t *out) {
 }
 
 }  // namespace
+
+void tl_release_ir_graphs(tl_ctx *ctx) {
+  if (!ctx->ir) return;
+  for (auto &gx : ctx->ir->graph)
+    if (gx) {
+      cudaGraphExecDestroy(gx);
+      gx = nullptr;
+    }
+}
 
 void tl_release_ir(tl_ctx *ctx) {
   if (!ctx->ir) return;
@@ -506,11 +553,27 @@ int tl_ir_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_resu
   while (rel >= p.eps && ctx->host_sc->iter < p.maxiters) {
     k_ir_start<<<1, 1, 0, ctx->stream>>>(ctx->F.sc, rr, IR_DELTA * IR_DELTA);
     CKL();
-    cudaGraphExec_t exec;
-    if ((rc = ir_graph(ctx, which, &exec))) return rc;
+    cudaGraphExec_t exec = nullptr;
+    if (!ctx->host_loop && (rc = ir_graph(ctx, which, &exec))) return rc;
     const int before = ctx->host_sc->iter;
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
-    CK(cudaGraphLaunch(exec, ctx->stream));
+    if (ctx->host_loop) {
+      // the same kernels launched from the host (see run_host_loop_cg)
+      float *a = which ? ir->pb : ir->p, *b = which ? ir->p : ir->pb;
+      for (;;) {
+        for (int k = 0; k < 8; ++k) {
+          launch_ir_w(ctx, a, b, 1);
+          launch_ir_ur(ctx, b, 1, 0, 0);
+          launch_ir_w(ctx, b, a, 1);
+          launch_ir_ur(ctx, a, 1, 0, 0);
+        }
+        CKL();
+        if ((rc = tl_read_scalars(ctx))) return rc;
+        if (ctx->host_sc->done) break;
+      }
+    } else {
+      CK(cudaGraphLaunch(exec, ctx->stream));
+    }
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     CK(cudaEventSynchronize(ctx->ev1));
     float t = 0.f;
@@ -557,4 +620,9 @@ int tl_ir_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch)
   CK(cudaEventElapsedTime(&t, ctx->tev0, ctx->tev1));
   *ms_per_launch = t / reps;
   return TL_OK;
+}
+
+tl::Walk *tl_ir_walk(tl_ctx *ctx, int kernel) {
+  if (ensure_ir(ctx)) return nullptr;
+  return kernel == 2 ? &ctx->ir->walk_w : &ctx->ir->walk_ur;
 }

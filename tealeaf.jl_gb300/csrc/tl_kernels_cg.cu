@@ -13,6 +13,7 @@
 // reference's operation order with no FMA (bit-identical to the CPU
 // restatement); otherwise the stencil is diag*p - kx1*pE - kx0*pW - ky1*pN -
 // ky0*pS with the diagonal read from memory and every update fused.
+#include "tl_solvers.h"
 #include "tl_walk.cuh"
 
 namespace tl {
@@ -42,7 +43,7 @@ struct OpRefW : NoSkip {
     DevScalars *sc = F.sc;
     sc->pw = tot[0];
     sc->alpha = ddiv(sc->rro, sc->pw);
-    F.cgalpha[sc->iter + 1] = sc->alpha;
+    if (sc->iter < sc->maxiters) F.cgalpha[sc->iter + 1] = sc->alpha;  // table holds maxiters + 2 entries
   }
 };
 
@@ -53,7 +54,7 @@ __device__ __forceinline__ void ur_epilogue(const Fields &F, double rrn, cudaGra
   DevScalars *sc = F.sc;
   sc->rrn = rrn;
   sc->beta = ddiv(rrn, sc->rro);
-  F.cgbeta[sc->iter + 1] = sc->beta;
+  if (sc->iter < sc->maxiters) F.cgbeta[sc->iter + 1] = sc->beta;
   if (!sc->stale_rro) sc->rro = rrn;
   sc->error = rrn;
   sc->iter += 1;
@@ -171,6 +172,33 @@ struct OpTlW {
     return make_double2(axpy<EXACT>(beta, pv.x, rv.x), axpy<EXACT>(beta, pv.y, rv.y));
   }
 
+  // Raw loads of one row (p and r of the lane's pair, the edge lanes' extra
+  // neighbour, kx, the diagonal), issued one row ahead of their use.
+  struct Row {
+    double2 p, r;  // the pair
+    double ep, er; // edge neighbour: i0-1 on lane 0, i0+2 on lane 31
+    double2 kx, dg;
+    double kxe;    // kx at i0+2 for the lanes that cannot take it from lane+1
+  };
+  __device__ __forceinline__ void load_row(Row &o, int i0, int j, bool valid, bool first, int edge_col) const {
+    if (!valid) return;
+    const size_t c = g.at(i0, j);
+    o.p = ld2(psrc + c);
+    if (!first) o.r = ld2(F.r + c);
+    if (edge_col >= 0) {
+      const size_t e = g.at(edge_col, j);
+      o.ep = __ldg(psrc + e);
+      if (!first) o.er = __ldg(F.r + e);
+    }
+  }
+  __device__ __forceinline__ void load_coef(Row &o, int i0, int j, bool valid, bool kx_edge) const {
+    if (!valid) return;
+    const size_t c = g.at(i0, j);
+    o.kx = ld2(F.kx + c);
+    if (!EXACT) o.dg = ld2(F.diag + c);
+    if (kx_edge) o.kxe = __ldg(F.kx + c + 2);
+  }
+
   __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
     const int nx = g.nx, ny = g.ny;
     const int lane = threadIdx.x & 31;
@@ -180,36 +208,54 @@ struct OpTlW {
     const double beta = F.sc->beta;
     const bool first = F.sc->first != 0;
     const double2 z = make_double2(0.0, 0.0);
+    // the edge lanes fetch the neighbour their shuffle cannot supply
+    const int edge_col = !valid ? -1 : (lane == 0 && i0 > 0) ? i0 - 1 : (lane == 31 && inner) ? i0 + 2 : -1;
+    const bool kx_edge = valid && has1 && (!inner || lane == 31);
+    auto pnew = [&](const Row &o) {
+      return first ? o.p : make_double2(axpy<EXACT>(beta, o.p.x, o.r.x), axpy<EXACT>(beta, o.p.y, o.r.y));
+    };
+    auto pnew_edge = [&](const Row &o) { return first ? o.ep : axpy<EXACT>(beta, o.ep, o.er); };
 
-    double2 pc = pn2(i0, j0, beta, first, valid);
-    double2 ps = (j0 > 0) ? pn2(i0, j0 - 1, beta, first, valid) : pc;  // reflect at j = 0
+    Row cur = {}, nxt = {}, tmp = {};
+    load_row(cur, i0, j0, valid, first, edge_col);
+    load_coef(cur, i0, j0, valid, kx_edge);
+    if (j0 > 0) load_row(tmp, i0, j0 - 1, valid, first, -1);
+    if (j0 + 1 < ny) load_row(nxt, i0, j0 + 1, valid, first, edge_col);
     double2 kyc = valid ? ld2(F.ky + g.at(i0, j0)) : z;
+    double2 kyn = valid ? ld2(F.ky + g.at(i0, j0 + 1)) : z;
+    double2 pc = valid ? pnew(cur) : z;
+    double2 ps = (j0 > 0 && valid) ? pnew(tmp) : pc;  // reflect at j = 0
     for (int j = j0; j < j1; ++j) {
-      const double2 pnn = (j + 1 < ny) ? pn2(i0, j + 1, beta, first, valid) : pc;  // reflect at j = ny-1
-      const double2 kyn = valid ? ld2(F.ky + g.at(i0, j + 1)) : z;
-      const double2 kx2 = valid ? ld2(F.kx + g.at(i0, j)) : z;
-      const double2 dg = (!EXACT && valid) ? ld2(F.diag + g.at(i0, j)) : z;
-      double pw = __shfl_up_sync(FULL, pc.y, 1);    // p' at i0-1
-      double pe = __shfl_down_sync(FULL, pc.x, 1);  // p' at i0+2
-      double kxe = __shfl_down_sync(FULL, kx2.x, 1);  // kx at i0+2
+      // issue the loads of the next row before this row's arithmetic
+      Row nn = {};
+      double2 kyn2 = z;
+      if (j + 1 < j1) {
+        if (j + 2 < ny) load_row(nn, i0, j + 2, valid, first, edge_col);
+        load_coef(nxt, i0, j + 1, valid, kx_edge);
+        kyn2 = valid ? ld2(F.ky + g.at(i0, j + 2)) : z;
+      }
+      const double2 pnn = (j + 1 < ny && valid) ? pnew(nxt) : pc;  // reflect at j = ny-1
+      double pw = __shfl_up_sync(FULL, pc.y, 1);         // p' at i0-1
+      double pe = __shfl_down_sync(FULL, pc.x, 1);       // p' at i0+2
+      double kxe = __shfl_down_sync(FULL, cur.kx.x, 1);  // kx at i0+2
       if (valid) {
         if (i0 == 0) pw = pc.x;                       // reflect at i = 0
-        else if (lane == 0) pw = pn1(i0 - 1, j, beta, first);
+        else if (lane == 0) pw = pnew_edge(cur);
         if (has1) {
           if (!inner) {
             pe = pc.y;                                // reflect at i = nx-1
-            kxe = __ldg(F.kx + g.at(i0 + 2, j));      // kx of the halo column
+            kxe = cur.kxe;                            // kx of the halo column
           } else if (lane == 31) {
-            pe = pn1(i0 + 2, j, beta, first);
-            kxe = __ldg(F.kx + g.at(i0 + 2, j));
+            pe = pnew_edge(cur);
+            kxe = cur.kxe;
           }
         }
         const double e0 = has1 ? pc.y : pc.x;
-        const double w0 = stencil<EXACT>(pc.x, e0, pw, pnn.x, ps.x, kx2.x, kx2.y, kyc.x, kyn.x, dg.x);
+        const double w0 = stencil<EXACT>(pc.x, e0, pw, pnn.x, ps.x, cur.kx.x, cur.kx.y, kyc.x, kyn.x, cur.dg.x);
         const size_t c = g.at(i0, j);
         acc[0] = acc_mul<EXACT>(acc[0], w0, pc.x);
         if (has1) {
-          const double w1 = stencil<EXACT>(pc.y, pe, pc.x, pnn.y, ps.y, kx2.y, kxe, kyc.y, kyn.y, dg.y);
+          const double w1 = stencil<EXACT>(pc.y, pe, pc.x, pnn.y, ps.y, cur.kx.y, kxe, kyc.y, kyn.y, cur.dg.y);
           acc[0] = acc_mul<EXACT>(acc[0], w1, pc.y);
           st2(F.w + c, make_double2(w0, w1));
           st2(pdst + c, pc);
@@ -221,13 +267,16 @@ struct OpTlW {
       ps = pc;
       pc = pnn;
       kyc = kyn;
+      kyn = kyn2;
+      cur = nxt;
+      nxt = nn;
     }
   }
   __device__ void fin(const double *tot) const {
     DevScalars *sc = F.sc;
     sc->pw = tot[0];
     sc->alpha = ddiv(sc->rro, sc->pw);
-    F.cgalpha[sc->iter + 1] = sc->alpha;
+    if (sc->iter < sc->maxiters) F.cgalpha[sc->iter + 1] = sc->alpha;  // table holds maxiters + 2 entries
   }
 };
 
@@ -293,6 +342,18 @@ struct OpTlP : NoSkip {
     }
   }
 };
+
+}  // namespace tl
+
+int tl_occupancy_cg(int kernel, int threads) {
+  int n = 0;
+  cudaError_t e = kernel == 0
+      ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, tl::k_walk<1, tl::OpTlW<false>>, threads, 0)
+      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, tl::k_walk<1, tl::OpTlUR<false>>, threads, 0);
+  return e == cudaSuccess ? n : 1;
+}
+
+namespace tl {
 
 void launch_tl_w(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk, const double *psrc, double *pdst,
                  int exact, int guard) {

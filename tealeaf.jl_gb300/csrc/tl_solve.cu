@@ -51,7 +51,7 @@ int tl_read_scalars(tl_ctx *ctx) {
 }
 
 const Walk &tl_walk_for(tl_ctx *ctx, int exact) {
-  return (ctx->cfg.mode == TL_MODE_REFERENCE || exact) ? ctx->walk_exact : ctx->walk_fast;
+  return (ctx->cfg.mode == TL_MODE_REFERENCE || exact) ? ctx->walk_exact : ctx->walk_ur64;
 }
 
 // CG.init! (CG.jl:47-79).  Also stores the fused kernels' diagonal.
@@ -98,11 +98,12 @@ static int record_body(tl_ctx *ctx, int which, cudaGraphConditionalHandle h) {
     case TL_GRAPH_CG_EXACT:
     case TL_GRAPH_CG_FAST: {
       const int exact = which == TL_GRAPH_CG_EXACT;
-      const Walk &wk = exact ? ctx->walk_exact : ctx->walk_fast;
-      launch_tl_w(st, F, g, wk, F.p, F.pb, exact, 0);
-      launch_tl_ur(st, F, g, wk, F.pb, exact, 0, h, 0);
-      launch_tl_w(st, F, g, wk, F.pb, F.p, exact, 1);
-      launch_tl_ur(st, F, g, wk, F.p, exact, 1, h, 1);
+      const Walk &ww = exact ? ctx->walk_exact : ctx->walk_w64;
+      const Walk &wu = exact ? ctx->walk_exact : ctx->walk_ur64;
+      launch_tl_w(st, F, g, ww, F.p, F.pb, exact, 0);
+      launch_tl_ur(st, F, g, wu, F.pb, exact, 0, h, 0);
+      launch_tl_w(st, F, g, ww, F.pb, F.p, exact, 1);
+      launch_tl_ur(st, F, g, wu, F.p, exact, 1, h, 1);
       break;
     }
     default:
@@ -167,13 +168,45 @@ void tl_release_graphs(tl_ctx *ctx) {
     }
 }
 
+// The same loop launched from the host: batches of eight two-iteration
+// bodies whose kernels all skip once the device has set `done`, with the flag
+// read back after each batch.  Profilers cannot see kernels inside graphs
+// that hold conditional nodes; this mode (TEALEAF_GB300_LOOP=host) runs the
+// identical kernels where they can.
+static int run_host_loop_cg(tl_ctx *ctx, int exact) {
+  const Fields &F = ctx->F;
+  const Geom &g = ctx->g;
+  const Walk &ww = exact ? ctx->walk_exact : ctx->walk_w64;
+  const Walk &wu = exact ? ctx->walk_exact : ctx->walk_ur64;
+  for (;;) {
+    for (int b = 0; b < 8; ++b) {
+      launch_tl_w(ctx->stream, F, g, ww, F.p, F.pb, exact, 1);
+      launch_tl_ur(ctx->stream, F, g, wu, F.pb, exact, 1, 0, 0);
+      launch_tl_w(ctx->stream, F, g, ww, F.pb, F.p, exact, 1);
+      launch_tl_ur(ctx->stream, F, g, wu, F.p, exact, 1, 0, 0);
+    }
+    CKL();
+    int rc = tl_read_scalars(ctx);
+    if (rc) return rc;
+    if (ctx->host_sc->done) return TL_OK;
+  }
+}
+
 // Runs one loop graph, timing it with events on the context stream.
 int tl_run_graph(tl_ctx *ctx, int which, double *ms) {
-  cudaGraphExec_t exec;
-  int rc = tl_get_graph(ctx, which, &exec);
-  if (rc) return rc;
+  const bool host = ctx->host_loop && (which == TL_GRAPH_CG_EXACT || which == TL_GRAPH_CG_FAST);
+  cudaGraphExec_t exec = nullptr;
+  if (!host) {
+    int rc = tl_get_graph(ctx, which, &exec);
+    if (rc) return rc;
+  }
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
-  CK(cudaGraphLaunch(exec, ctx->stream));
+  if (host) {
+    int rc = run_host_loop_cg(ctx, which == TL_GRAPH_CG_EXACT);
+    if (rc) return rc;
+  } else {
+    CK(cudaGraphLaunch(exec, ctx->stream));
+  }
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
   CK(cudaEventSynchronize(ctx->ev1));
   float t = 0.f;
@@ -183,22 +216,97 @@ int tl_run_graph(tl_ctx *ctx, int which, double *ms) {
 }
 
 // ---------------------------------------------------------------------------
-// autotuned walk of the fused kernels
+// walk layouts and the autotuner
 // ---------------------------------------------------------------------------
 
-Walk tl_tune_walk(tl_ctx *ctx) {
-  const Geom &g = ctx->g;
+// Rows per tile chosen so that the tiles spread evenly over `blocks`
+// persistent blocks: minimise the rows the busiest block walks (one extra
+// neighbour row re-read per tile), preferring longer tiles on ties.
+Walk tl_walk_balanced(int nx, int ny, int cols_per_warp, int warps, int blocks) {
   Walk w;
-  w.warps = 8;
-  w.rows = 32;
-  const int TW = 64 * w.warps;
-  w.ntx = (g.nx + TW - 1) / TW;
-  const int nty = (g.ny + w.rows - 1) / w.rows;
-  w.tiles = w.ntx * nty;
-  const int cap = 3 * ctx->sm_count;
-  w.blocks = w.tiles < cap ? w.tiles : cap;
+  w.warps = warps;
+  const int TW = cols_per_warp * warps;
+  w.ntx = (nx + TW - 1) / TW;
+  long long best_cost = -1;
+  int best_rows = 1;
+  const int rmax = ny < 1024 ? ny : 1024;
+  for (int rows = 4 < ny ? 4 : ny; rows <= rmax; ++rows) {
+    const long long nty = (ny + rows - 1) / rows, tiles = (long long)w.ntx * nty;
+    const long long per = (tiles + blocks - 1) / blocks;
+    const long long cost = per * (rows + 1);
+    if (best_cost < 0 || cost < best_cost || (cost == best_cost && rows > best_rows)) {
+      best_cost = cost;
+      best_rows = rows;
+    }
+  }
+  w.rows = best_rows;
+  w.tiles = w.ntx * ((ny + best_rows - 1) / best_rows);
+  w.blocks = w.tiles < blocks ? w.tiles : blocks;
   if (w.blocks < 1) w.blocks = 1;
   return w;
+}
+
+// A walk with fixed rows per tile: tiles in row-major order, so that the
+// blocks running at one time sweep neighbouring tiles of the same rows.
+static Walk walk_fixed(int nx, int ny, int cols_per_warp, int warps, int rows, int blocks) {
+  Walk w;
+  w.warps = warps;
+  w.rows = rows;
+  const int TW = cols_per_warp * warps;
+  w.ntx = (nx + TW - 1) / TW;
+  w.tiles = w.ntx * ((ny + rows - 1) / rows);
+  w.blocks = w.tiles < blocks ? w.tiles : blocks;
+  if (w.blocks < 1) w.blocks = 1;
+  return w;
+}
+
+// Candidates: 4 or 8 warps per block; 2..8 resident blocks per SM (within the
+// kernel's occupancy); tiles of 8, 16 or 32 rows, or the balanced length.
+// Short tiles keep the blocks that run together inside the same DRAM rows;
+// the balanced length gives one long tile per block.  Each candidate runs
+// twice untimed and three times under CUDA events on the context stream.
+Walk tl_autotune(tl_ctx *ctx, int cols_per_warp, int occ4, int occ8, void (*launch)(tl_ctx *, const tl::Walk &)) {
+  const Geom &g = ctx->g;
+  Walk best = walk_fixed(g.nx, g.ny, cols_per_warp, 8, 16, 3 * ctx->sm_count);
+  float best_ms = -1.f;
+  for (int warps = 4; warps <= 8; warps += 4) {
+    const int occ = warps == 4 ? occ4 : occ8;
+    for (int bps = 2; bps <= occ && bps <= 8; ++bps) {
+      const int B = bps * ctx->sm_count;
+      if (B > ctx->max_blocks) break;
+      const Walk cands[4] = {walk_fixed(g.nx, g.ny, cols_per_warp, warps, 8, B),
+                             walk_fixed(g.nx, g.ny, cols_per_warp, warps, 16, B),
+                             walk_fixed(g.nx, g.ny, cols_per_warp, warps, 32, B),
+                             tl_walk_balanced(g.nx, g.ny, cols_per_warp, warps, B)};
+      bool grid_full = false;
+      for (const Walk &w : cands) {
+        if (w.blocks < B) grid_full = true;  // fewer tiles than blocks: more blocks per SM cannot help
+        launch(ctx, w);
+        launch(ctx, w);
+        if (cudaEventRecord(ctx->tev0, ctx->stream) != cudaSuccess) return best;
+        for (int k = 0; k < 3; ++k) launch(ctx, w);
+        if (cudaEventRecord(ctx->tev1, ctx->stream) != cudaSuccess) return best;
+        if (cudaEventSynchronize(ctx->tev1) != cudaSuccess) return best;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->tev0, ctx->tev1);
+        if (best_ms < 0.f || ms < best_ms) {
+          best_ms = ms;
+          best = w;
+        }
+      }
+      if (grid_full) break;
+    }
+  }
+  cudaGetLastError();
+  return best;
+}
+
+void tl_launch_w64_for_tuning(tl_ctx *ctx, const Walk &wk) {
+  launch_tl_w(ctx->stream, ctx->F, ctx->g, wk, ctx->F.p, ctx->F.pb, 0, 0);
+}
+
+void tl_launch_ur64_for_tuning(tl_ctx *ctx, const Walk &wk) {
+  launch_tl_ur(ctx->stream, ctx->F, ctx->g, wk, ctx->F.pb, 0, 0, 0, 0);
 }
 
 // ---------------------------------------------------------------------------

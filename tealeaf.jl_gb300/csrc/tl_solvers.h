@@ -27,9 +27,13 @@ struct tl_ctx {
   int device = 0, sm_count = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  tl::Walk walk_exact{}, walk_fast{};
+  tl::Walk walk_exact{};            // fixed layout of the bit-reproducible kernels
+  tl::Walk walk_w64{}, walk_ur64{};  // autotuned layouts of the fused FP64 CG kernels
+  int max_blocks = 0;                // capacity of the reduction partials
+  int host_loop = 0;                 // iteration loops launched from the host (TEALEAF_GB300_LOOP=host)
   double *buf = nullptr;
   void *small = nullptr;
+  size_t buf_bytes = 0, small_bytes = 0;
   tl::Fields F{};
   double *field_ptr[TL_NFIELDS] = {};
   tl::DevScalars *host_sc = nullptr;
@@ -48,9 +52,17 @@ int tl_cuda_fail(tl_ctx *ctx, cudaError_t e, const char *what, int line);
 double *tl_exchange_ptr(tl_ctx *ctx, int ex);
 int tl_marked(tl_ctx *ctx, double **ptrs);
 int tl_halo_check(tl_ctx *ctx, int depth);
-tl::Walk tl_tune_walk(tl_ctx *ctx);
+tl::Walk tl_walk_balanced(int nx, int ny, int cols_per_warp, int warps, int blocks);
+// Times candidate walks of one kernel (`launch` runs it once with a walk) and
+// returns the fastest; occ4/occ8 are the kernel's resident blocks per SM at 4
+// and 8 warps per block.
+tl::Walk tl_autotune(tl_ctx *ctx, int cols_per_warp, int occ4, int occ8, void (*launch)(tl_ctx *, const tl::Walk &));
+int tl_occupancy_cg(int kernel, int threads);  // 0: fused W, 1: fused UR (FP64)
+void tl_launch_w64_for_tuning(tl_ctx *ctx, const tl::Walk &wk);
+void tl_launch_ur64_for_tuning(tl_ctx *ctx, const tl::Walk &wk);
 void tl_release_graphs(tl_ctx *ctx);
 void tl_release_ir(tl_ctx *ctx);
+void tl_release_ir_graphs(tl_ctx *ctx);
 
 // shared solver pieces (tl_solve.cu)
 int tl_set_loop_params(tl_ctx *ctx, const tl_params *prm, int switch_rule, int stale_rro);
@@ -68,6 +80,7 @@ int tl_ppcg_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_re
 int tl_jacobi_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res);
 int tl_ir_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res);
 int tl_ir_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch);
+tl::Walk *tl_ir_walk(tl_ctx *ctx, int kernel);  // the FP32 kernels' layouts (kernel 2, 3)
 
 #define CK(x)                                                     \
   do {                                                            \
