@@ -104,10 +104,28 @@ void launch_ref_ur(cudaStream_t st, const Fields &F, const Geom &g, const Walk &
                    int set_cond);
 void launch_ref_p(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk);
 void launch_tl_w(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk, const double *psrc, double *pdst,
-                 int exact, int guard);
+                 int exact, int guard, int store_coef = 1);
 void launch_tl_ur(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk, const double *p, int exact,
                   int guard, cudaGraphConditionalHandle cond, int set_cond);
 void launch_tl_p(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk, const double *psrc, double *pdst,
                  int exact);
+
+// Chebyshev, PPCG and Jacobi kernels (tl_kernels_cheby.cu)
+void launch_cheby_init(cudaStream_t st, const Fields &F, const Geom &g, double theta);
+void launch_cheby_step(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk, const double *usrc,
+                       double *udst, int exact, int guard, int force_norm, cudaGraphConditionalHandle cond,
+                       int set_cond);
+void launch_ppcg_ur(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk, const double *p, double *sd,
+                    int exact, int guard);
+void launch_ppcg_inner(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk, const double *sdsrc,
+                       double *sddst, int pp, int last, int exact, int guard, cudaGraphConditionalHandle cond,
+                       int set_cond);
+void launch_jacobi(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk, const double *usrc, double *udst,
+                   int guard);
+void launch_jacobi_check(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk, const double *u, int guard,
+                         cudaGraphConditionalHandle cond, int set_cond);
+void launch_norm_r(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk);
+void launch_ppcg_sd_final(cudaStream_t st, const Fields &F, const Geom &g, const double *fin, const double *prev);
+void launch_copy_interior(cudaStream_t st, double *dst, const double *src, const Geom &g);
 
 }  // namespace tl

@@ -14,7 +14,7 @@
 // restatement); otherwise the stencil is diag*p - kx1*pE - kx0*pW - ky1*pN -
 // ky0*pS with the diagonal read from memory and every update fused.
 #include "tl_solvers.h"
-#include "tl_walk.cuh"
+#include "tl_march.cuh"
 
 namespace tl {
 
@@ -131,152 +131,43 @@ void launch_ref_p(cudaStream_t st, const Fields &F, const Geom &g, const Walk &w
 // ---------------------------------------------------------------------------
 
 template <bool EXACT>
-__device__ __forceinline__ double stencil(double c, double e, double w, double n, double s, double kx0, double kx1,
-                                          double ky0, double ky1, double dg) {
-  if (EXACT) {
-    const double consum = dadd(dadd(dadd(dadd(1.0, kx1), kx0), ky1), ky0);
-    double v = dmul(consum, c);
-    v = dsub(v, dadd(dmul(kx1, e), dmul(kx0, w)));
-    v = dsub(v, dadd(dmul(ky1, n), dmul(ky0, s)));
-    return v;
-  }
-  double t = dg * c;
-  t = fma(-kx1, e, t);
-  t = fma(-kx0, w, t);
-  t = fma(-ky1, n, t);
-  t = fma(-ky0, s, t);
-  return t;
-}
-
-template <bool EXACT>
 struct OpTlW {
   Fields F;
   Geom g;
   const double *__restrict__ psrc;
   double *__restrict__ pdst;
   int guard;
+  int store_coef;  // CG and its presteps record alpha in cgalpha (CG.jl:37); PPCG's outer steps do not
   __device__ bool skip() const { return guard && F.sc->done; }
   __device__ void on_skip() const {}
 
-  __device__ __forceinline__ double pn1(int i, int j, double beta, bool first) const {
-    const size_t c = g.at(i, j);
-    const double pv = __ldg(psrc + c);
-    return first ? pv : axpy<EXACT>(beta, pv, __ldg(F.r + c));
-  }
-  __device__ __forceinline__ double2 pn2(int i0, int j, double beta, bool first, bool valid) const {
-    if (!valid) return make_double2(0.0, 0.0);
-    const size_t c = g.at(i0, j);
-    const double2 pv = ld2(psrc + c);
-    if (first) return pv;
-    const double2 rv = ld2(F.r + c);
-    return make_double2(axpy<EXACT>(beta, pv.x, rv.x), axpy<EXACT>(beta, pv.y, rv.y));
-  }
-
-  // Raw loads of one row (p and r of the lane's pair, the edge lanes' extra
-  // neighbour, kx, the diagonal), issued one row ahead of their use.
-  struct Row {
-    double2 p, r;  // the pair
-    double ep, er; // edge neighbour: i0-1 on lane 0, i0+2 on lane 31
-    double2 kx, dg;
-    double kxe;    // kx at i0+2 for the lanes that cannot take it from lane+1
-  };
-  __device__ __forceinline__ void load_row(Row &o, int i0, int j, bool valid, bool first, int edge_col) const {
-    if (!valid) return;
-    const size_t c = g.at(i0, j);
-    o.p = ld2(psrc + c);
-    if (!first) o.r = ld2(F.r + c);
-    if (edge_col >= 0) {
-      const size_t e = g.at(edge_col, j);
-      o.ep = __ldg(psrc + e);
-      if (!first) o.er = __ldg(F.r + e);
-    }
-  }
-  __device__ __forceinline__ void load_coef(Row &o, int i0, int j, bool valid, bool kx_edge) const {
-    if (!valid) return;
-    const size_t c = g.at(i0, j);
-    o.kx = ld2(F.kx + c);
-    if (!EXACT) o.dg = ld2(F.diag + c);
-    if (kx_edge) o.kxe = __ldg(F.kx + c + 2);
-  }
-
   __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
-    const int nx = g.nx, ny = g.ny;
-    const int lane = threadIdx.x & 31;
-    const bool valid = i0 < nx;     // the lane owns cell i0
-    const bool has1 = i0 + 1 < nx;  // ... and cell i0+1
-    const bool inner = i0 + 2 < nx; // cell i0+1 has an interior east neighbour
-    const double beta = F.sc->beta;
-    const bool first = F.sc->first != 0;
-    const double2 z = make_double2(0.0, 0.0);
-    // the edge lanes fetch the neighbour their shuffle cannot supply
-    const int edge_col = !valid ? -1 : (lane == 0 && i0 > 0) ? i0 - 1 : (lane == 31 && inner) ? i0 + 2 : -1;
-    const bool kx_edge = valid && has1 && (!inner || lane == 31);
-    auto pnew = [&](const Row &o) {
-      return first ? o.p : make_double2(axpy<EXACT>(beta, o.p.x, o.r.x), axpy<EXACT>(beta, o.p.y, o.r.y));
-    };
-    auto pnew_edge = [&](const Row &o) { return first ? o.ep : axpy<EXACT>(beta, o.ep, o.er); };
-
-    Row cur = {}, nxt = {}, tmp = {};
-    load_row(cur, i0, j0, valid, first, edge_col);
-    load_coef(cur, i0, j0, valid, kx_edge);
-    if (j0 > 0) load_row(tmp, i0, j0 - 1, valid, first, -1);
-    if (j0 + 1 < ny) load_row(nxt, i0, j0 + 1, valid, first, edge_col);
-    double2 kyc = valid ? ld2(F.ky + g.at(i0, j0)) : z;
-    double2 kyn = valid ? ld2(F.ky + g.at(i0, j0 + 1)) : z;
-    double2 pc = valid ? pnew(cur) : z;
-    double2 ps = (j0 > 0 && valid) ? pnew(tmp) : pc;  // reflect at j = 0
-    for (int j = j0; j < j1; ++j) {
-      // issue the loads of the next row before this row's arithmetic
-      Row nn = {};
-      double2 kyn2 = z;
-      if (j + 1 < j1) {
-        if (j + 2 < ny) load_row(nn, i0, j + 2, valid, first, edge_col);
-        load_coef(nxt, i0, j + 1, valid, kx_edge);
-        kyn2 = valid ? ld2(F.ky + g.at(i0, j + 2)) : z;
-      }
-      const double2 pnn = (j + 1 < ny && valid) ? pnew(nxt) : pc;  // reflect at j = ny-1
-      double pw = __shfl_up_sync(FULL, pc.y, 1);         // p' at i0-1
-      double pe = __shfl_down_sync(FULL, pc.x, 1);       // p' at i0+2
-      double kxe = __shfl_down_sync(FULL, cur.kx.x, 1);  // kx at i0+2
-      if (valid) {
-        if (i0 == 0) pw = pc.x;                       // reflect at i = 0
-        else if (lane == 0) pw = pnew_edge(cur);
-        if (has1) {
-          if (!inner) {
-            pe = pc.y;                                // reflect at i = nx-1
-            kxe = cur.kxe;                            // kx of the halo column
-          } else if (lane == 31) {
-            pe = pnew_edge(cur);
-            kxe = cur.kxe;
-          }
-        }
-        const double e0 = has1 ? pc.y : pc.x;
-        const double w0 = stencil<EXACT>(pc.x, e0, pw, pnn.x, ps.x, cur.kx.x, cur.kx.y, kyc.x, kyn.x, cur.dg.x);
-        const size_t c = g.at(i0, j);
-        acc[0] = acc_mul<EXACT>(acc[0], w0, pc.x);
-        if (has1) {
-          const double w1 = stencil<EXACT>(pc.y, pe, pc.x, pnn.y, ps.y, cur.kx.y, kxe, kyc.y, kyn.y, cur.dg.y);
-          acc[0] = acc_mul<EXACT>(acc[0], w1, pc.y);
-          st2(F.w + c, make_double2(w0, w1));
-          st2(pdst + c, pc);
-        } else {
-          F.w[c] = w0;
-          pdst[c] = pc.x;
-        }
-      }
-      ps = pc;
-      pc = pnn;
-      kyc = kyn;
-      kyn = kyn2;
-      cur = nxt;
-      nxt = nn;
-    }
+    SrcPUpdate<EXACT> src;
+    src.p = psrc;
+    src.r = F.r;
+    src.beta = F.sc->beta;
+    src.first = F.sc->first != 0;
+    march<!EXACT>(g, F.kx, F.ky, F.diag, src, i0, j0, j1,
+                  [&](int j, const Nbr &c0, const Nbr &c1, bool has1, double2 pc) {
+                    const size_t c = g.at(i0, j);
+                    const double w0 = apply_a<EXACT>(c0);
+                    acc[0] = acc_mul<EXACT>(acc[0], w0, c0.c);
+                    if (has1) {
+                      const double w1 = apply_a<EXACT>(c1);
+                      acc[0] = acc_mul<EXACT>(acc[0], w1, c1.c);
+                      st2(F.w + c, make_double2(w0, w1));
+                      st2(pdst + c, pc);
+                    } else {
+                      F.w[c] = w0;
+                      pdst[c] = pc.x;
+                    }
+                  });
   }
   __device__ void fin(const double *tot) const {
     DevScalars *sc = F.sc;
     sc->pw = tot[0];
     sc->alpha = ddiv(sc->rro, sc->pw);
-    if (sc->iter < sc->maxiters) F.cgalpha[sc->iter + 1] = sc->alpha;  // table holds maxiters + 2 entries
+    if (store_coef && sc->iter < sc->maxiters) F.cgalpha[sc->iter + 1] = sc->alpha;  // table holds maxiters + 2 entries
   }
 };
 
@@ -356,14 +247,14 @@ int tl_occupancy_cg(int kernel, int threads) {
 namespace tl {
 
 void launch_tl_w(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk, const double *psrc, double *pdst,
-                 int exact, int guard) {
+                 int exact, int guard, int store_coef) {
   if (exact) {
     OpTlW<true> op;
-    op.F = F; op.g = g; op.psrc = psrc; op.pdst = pdst; op.guard = guard;
+    op.F = F; op.g = g; op.psrc = psrc; op.pdst = pdst; op.guard = guard; op.store_coef = store_coef;
     launch_walk<1>(st, op, wk, g.ny);
   } else {
     OpTlW<false> op;
-    op.F = F; op.g = g; op.psrc = psrc; op.pdst = pdst; op.guard = guard;
+    op.F = F; op.g = g; op.psrc = psrc; op.pdst = pdst; op.guard = guard; op.store_coef = store_coef;
     launch_walk<1>(st, op, wk, g.ny);
   }
 }

@@ -2,7 +2,7 @@
 // finalise and field summary kernels.  Every arithmetic step uses explicitly
 // rounded double operations (no FMA contraction) in the reference's order, so
 // these kernels are bit-identical to the CPU restatement of the reference.
-#include "tl_walk.cuh"
+#include "tl_march.cuh"
 
 namespace tl {
 
@@ -234,17 +234,6 @@ __global__ void k_init_diag(Fields F, Geom g) {
 
 void launch_init_diag(cudaStream_t st, const Fields &F, const Geom &g) {
   k_init_diag<<<grid_for((long long)g.nx * g.ny, 256), 256, 0, st>>>(F, g);
-}
-
-// smvp (kernels.jl:178-184) on memory values, reference order, no FMA.
-__device__ __forceinline__ double smvp_exact(const Fields &F, const Geom &g, const double *a, size_t c, int mode) {
-  const double kxr = F.kx[c + 1], kxc = F.kx[c], kyt = F.ky[c + g.pitch], kyc = F.ky[c];
-  const double consum = dadd(dadd(dadd(dadd(1.0, kxr), kxc), kyt), kyc);
-  double v = dmul(consum, a[c]);
-  if (mode == TL_MODE_REFERENCE) return v;  // kernels.jl:181 returns here
-  v = dsub(v, dadd(dmul(kxr, a[c + 1]), dmul(kxc, a[c - 1])));
-  v = dsub(v, dadd(dmul(kyt, a[c + g.pitch]), dmul(kyc, a[c - g.pitch])));
-  return v;
 }
 
 // Interior: w = A u, r = u - w, p = r, rro = sum r^2 (CG.jl:70-78).

@@ -2,6 +2,7 @@
 // (src/solvers/CG.jl:7-29) and the shared pieces of the other solvers:
 // tea_leaf_init, loop parameters, and the while-node iteration graphs.
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "tl_solvers.h"
@@ -267,7 +268,10 @@ static Walk walk_fixed(int nx, int ny, int cols_per_warp, int warps, int rows, i
 // twice untimed and three times under CUDA events on the context stream.
 Walk tl_autotune(tl_ctx *ctx, int cols_per_warp, int occ4, int occ8, void (*launch)(tl_ctx *, const tl::Walk &)) {
   const Geom &g = ctx->g;
-  Walk best = walk_fixed(g.nx, g.ny, cols_per_warp, 8, 16, 3 * ctx->sm_count);
+  // without tuning (TEALEAF_GB300_TUNE=0): 8 warps, 8-row tiles, 3 blocks per SM
+  Walk best = walk_fixed(g.nx, g.ny, cols_per_warp, 8, 8, 3 * ctx->sm_count);
+  const char *tune = getenv("TEALEAF_GB300_TUNE");
+  if (tune && !strcmp(tune, "0")) return best;
   float best_ms = -1.f;
   for (int warps = 4; warps <= 8; warps += 4) {
     const int occ = warps == 4 ? occ4 : occ8;

@@ -9,11 +9,11 @@ enum {
   TL_GRAPH_CG_REF_NOHALO,    // reference-mode CG step without the halo (Cheby/PPCG presteps)
   TL_GRAPH_CG_EXACT,         // tealeaf fused CG, reference operation order
   TL_GRAPH_CG_FAST,          // tealeaf fused CG, FMA
-  TL_GRAPH_CHEBY_EXACT,
+  TL_GRAPH_CHEBY_EXACT,      // Chebyshev steps, the first of the pair reading ub
   TL_GRAPH_CHEBY_FAST,
-  TL_GRAPH_JACOBI_EXACT,
-  TL_GRAPH_JACOBI_FAST,
-  TL_GRAPH_IR_INNER,         // FP32 inner CG of the refinement loop
+  TL_GRAPH_PPCG_EXACT,       // two PPCG outer steps with their inner sweeps
+  TL_GRAPH_PPCG_FAST,
+  TL_GRAPH_JACOBI,           // two Jacobi sweeps with their every-50th residual checks
   TL_NGRAPH
 };
 
@@ -43,6 +43,7 @@ struct tl_ctx {
   long long launches = 0;     // kernels launched by the current solve
   cudaEvent_t tev0 = nullptr, tev1 = nullptr;  // user timer
   cudaGraphExec_t graph[TL_NGRAPH] = {};
+  int ppcg_graph_inner = -1;  // inner sweeps recorded in the PPCG graphs
   tl_ir_state *ir = nullptr;
   char msg[512] = {};
 };

@@ -13,6 +13,7 @@ ROOT = Path(__file__).resolve().parents[1]
 PKG_DIR = ROOT / "tealeaf.jl_gb300"
 sys.path.insert(0, str(ROOT / "oracle"))
 sys.path.insert(0, str(Path(__file__).resolve().parent))
+sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
 
 
 def load_package():

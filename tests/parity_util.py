@@ -11,7 +11,7 @@ import oracle as O
 GOLDEN = Path(__file__).resolve().parent / "golden"
 CONFIG1 = (GOLDEN / "tea_config1.in").read_text()
 
-FIELDS = ["density", "energy0", "energy", "u", "u0", "p", "r", "w", "kx", "ky"]
+FIELDS = ["density", "energy0", "energy", "u", "u0", "p", "r", "w", "kx", "ky", "sd"]
 SOLVER_CODES = {"cg": 0, "cheby": 1, "ppcg": 2, "jacobi": 3}
 
 

@@ -1,0 +1,98 @@
+"""CPU tests of the host side: the deck reader of the host mirror against the
+oracle's restatement of src/settings.jl, and the C ABI library's exports
+(every entry point declared in include/tealeaf_gb300.h) without compute calls."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+import oracle as O
+from conftest import load_package
+from parity_util import CONFIG1, random_deck
+
+ROOT = Path(__file__).resolve().parents[1]
+
+DECKS = [
+    CONFIG1,
+    random_deck(64, 3, ny=40, steps=4, eps=1e-9, solver="ppcg", presteps=12),
+    # underscores stripped, the initial_timestep alias, a comment, unknown and malformed keys
+    "*tea\nx_cells = 20\ny_cells=20\nxmax=5.0\nymax=5.0\ninitial_timestep=0.01\nend_step=3\n"
+    "tl_max_iters=77\nmax_iters=500\nbogus=3\neps=1e-12\nerror_switch=true\neps_lim=1e-4\nuse_cheby\n"
+    "pres_teps=7\nhalo_depth=2\ncoefficient=2\ncheck_result=0\n"
+    "state 1 density=1.0 energy=1.0\n"
+    "state 2 density=2.5 energy=3.0 geometry=circular xmin=2.5 ymin=2.5 radius=1.0\n"
+    "state 3 density=0.5 energy=9.0 geometry=point xmin=1.0 ymin=1.0\n"
+    "max_iters=12.5\n",
+    # states after the size keys: the inset still uses the default dx
+    "x_cells=50\ny_cells=50\nxmax=10.0\nymax=10.0\nend_step=1\n"
+    "state 1 density=100.0 energy=0.0001\nstate 2 density=0.1 energy=25 geometry=rectangle xmin=1 xmax=3 "
+    "ymin=2 ymax=4\nuse_jacobi\n",
+]
+
+INT_KEYS = ["endstep", "presteps", "maxiters", "coefficient", "ppcginnersteps", "summaryfrequency", "halodepth",
+            "xcells", "ycells"]
+F_KEYS = ["eps", "dtinit", "endtime", "epslim", "xmin", "ymin", "xmax", "ymax", "dx", "dy"]
+
+
+@pytest.mark.parametrize("text", DECKS)
+def test_host_reader_matches_oracle(text):
+    tl = load_package()
+    h = tl.Settings.from_text(text)
+    o = O.parse_deck(text)
+    for k in INT_KEYS + F_KEYS:
+        assert getattr(h, k) == getattr(o, k), k
+    assert int(h.errorswitch) == o.errorswitch and int(h.checkresult) == o.checkresult
+    assert h.solver == o.solver
+    assert len(h.states) == o.nstates
+    for k, st in enumerate(h.states):
+        os = o.states[k]
+        for f in ("density", "energy", "xmin", "ymin", "xmax", "ymax", "radius", "geometry", "given", "pdx", "pdy"):
+            assert getattr(st, f) == getattr(os, f), (k, f)
+        for mode in (0, 1):
+            assert st.bounds(h, mode) == O.effective_bounds(o, k, mode)
+
+
+def test_reader_rejects_malformed_state():
+    tl = load_package()
+    bad = "state 1 density=1.0 energy\n"
+    with pytest.raises(ValueError):
+        tl.Settings.from_text(bad)
+    with pytest.raises(O.OracleError):
+        O.parse_deck(bad)
+
+
+def test_checkingvalue(tmp_path):
+    tl = load_package()
+    p = tmp_path / "tea.problems"
+    p.write_text("10 10 10 77.4067653961985\n4096 4096 10 1.0\n")
+    s = tl.Settings.from_text(CONFIG1)
+    from tealeaf_gb300.settings import checkingvalue, qa_passes
+    assert checkingvalue(s, str(p)) == 77.4067653961985
+    assert qa_passes(77.4067653961985 * (1 + 1e-6), 77.4067653961985)
+    assert not qa_passes(77.5, 77.4067653961985)
+
+
+def _declared_functions():
+    hdr = (ROOT / "include" / "tealeaf_gb300.h").read_text()
+    body = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:int|const char \*)\s*(tl_\w+)\s*\(", body, flags=re.M)))
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    names = _declared_functions()
+    assert len(names) >= 20
+    lib = C.CDLL(str(built_lib))
+    for n in names:
+        assert hasattr(lib, n), n
+    tl = load_package()
+    assert set(names) == set(tl._abi.SIGNATURES), set(names) ^ set(tl._abi.SIGNATURES)
+
+
+def test_library_loads_through_binding(built_lib):
+    tl = load_package()
+    lib = tl._abi.load()
+    assert lib.tl_last_error(None) == b"null context"
+    assert lib.tl_destroy(None) == 0
+    ctx = C.c_void_p()
+    assert lib.tl_create(C.byref(ctx), None) == 1       # null configuration: rejected before any CUDA call
