@@ -211,6 +211,11 @@ def run_e2e(tl, n, precision, steps, warmup):
 
 KERNELS = {"fp64": ((0, "cg_w_step", W_STEP_BYTES), (1, "cg_ur_step", UR_STEP_BYTES)),
            "fp32_ir": ((2, "ir_w_step", 24), (3, "ir_ur_step", 24))}
+# DRAM bytes (read + write) per interior cell of one launch, from the ncu
+# captures at 4096^2 summarised in profiles/*_4096.md; traffic grows with the
+# cells, so a full launch moves this times n^2.
+TRAFFIC_BYTES_PER_CELL = {"ir_w_step": 381.0e6 / 4096 ** 2, "ir_ur_step": 358.5e6 / 4096 ** 2,
+                          "cg_w_step": 923.7e6 / 4096 ** 2}
 
 
 def kernel_roofline(tl, chunk, variant):
@@ -359,8 +364,12 @@ def gpu_arm(args):
     if roof:
         dom = max(roof.values(), key=lambda d: d["ms"])
         dname = [k for k, v in roof.items() if v is dom][0]
+        tpc = TRAFFIC_BYTES_PER_CELL.get(dname)
         line["roofline"] = {"bound": "hbm", "kernel": dname, "achieved": dom["gbs"], "peak": peak,
-                            "unit": "GB/s", "frac": dom["gbs"] / peak, "traffic": None,
+                            "unit": "GB/s", "frac": dom["gbs"] / peak,
+                            "traffic": tpc * n * n if tpc else None,
+                            "traffic_source": "ncu capture at 4096^2 scaled by cells" if tpc else None,
+                            "algorithmic_bytes": dom["bytes_per_cell"] * n * n,
                             "peak_kind": peak_kind, "kernels": roof}
     if rank == 0 and world == 1 and not args.no_cpu:
         oracle = load_oracle()
@@ -379,6 +388,83 @@ def gpu_arm(args):
         dist.destroy_process_group()
 
 
+CONFIG2_STATES = """state 1 density=100.0 energy=0.0001
+state 2 density=0.1 energy=25.0 geometry=rectangle xmin=0.0 xmax=1.0 ymin=1.0 ymax=2.0
+state 3 density=0.1 energy=0.1 geometry=rectangle xmin=1.0 xmax=6.0 ymin=1.0 ymax=2.0
+state 4 density=0.1 energy=0.1 geometry=rectangle xmin=5.0 xmax=6.0 ymin=1.0 ymax=8.0
+state 5 density=0.1 energy=0.1 geometry=rectangle xmin=5.0 xmax=10.0 ymin=7.0 ymax=8.0
+"""
+# algorithmic bytes per interior cell of each timed kernel
+CONFIG2_KERNELS = ((0, "cg_w_step", 48), (1, "cg_ur_step", 48), (4, "cheby_step", 72), (5, "ppcg_inner_sweep", 64))
+
+
+def config2_deck(n: int, solver: str) -> str:
+    return CONFIG2_STATES + (f"x_cells={n}\ny_cells={n}\nxmin=0.0\nymin=0.0\nxmax=10.0\nymax=10.0\n"
+                             f"initial_timestep=0.004\nend_step=10\nmax_iters=40000\nuse_{solver}\neps=1e-10\n"
+                             "halo_depth=2\ncoefficient=1\nsummary_frequency=10\npresteps=30\nppcg_inner_steps=10\n")
+
+
+def run_config2(args):
+    """The 5-state geometry of the 10x10 deck on 4096^2 cells: CG, Chebyshev
+    (30 CG presteps) and PPCG (10 inner steps), 10 timesteps each at eps 1e-10
+    with each solver's own convergence test, three runs of each; per-kernel
+    HBM GB/s of the fused kernels on the solved fields; the CPU path's CG
+    per-iteration time beside it."""
+    import torch
+    torch.cuda.set_device(0)
+    tl = load_package()
+    n = args.size if args.size != 8192 else 4096
+    peak, peak_kind = measured_peaks()
+    out = {"workload": f"config2: 5-state geometry on {n}^2, 10 steps, eps 1e-10", "n": n, "solvers": {}}
+    for solver in ("cg", "cheby", "ppcg"):
+        runs = []
+        chunk = None
+        for run in range(3):
+            if chunk is not None:
+                chunk.close()
+            s = tl.Settings.from_text(config2_deck(n, solver), mode=1, exact=False)
+            chunk = tl.initialiseapp(s)
+            lib = chunk.lib
+            chunk.check(lib.tl_synchronize(chunk.ctx))
+            chunk.check(lib.tl_timer_start(chunk.ctx))
+            steps, sums = tl.diffuse(chunk, s, problemfile=None)
+            ms = C.c_double()
+            chunk.check(lib.tl_timer_stop(chunk.ctx, C.byref(ms)))
+            runs.append({"ms": ms.value, "iters": [r.iters for r in steps], "cg_iters": [r.cg_iters for r in steps],
+                         "inner_iters": [r.inner_iters for r in steps], "summary": sums[-1]})
+        kern = {}
+        for k, name, b in CONFIG2_KERNELS:
+            kms = C.c_double()
+            chunk.check(chunk.lib.tl_bench_kernel(chunk.ctx, k, 10, C.byref(kms)))
+            kern[name] = {"ms": kms.value, "gbs": b * n * n / (kms.value * 1e-3) / 1e9,
+                          "frac": b * n * n / (kms.value * 1e-3) / 1e9 / peak}
+        chunk.close()
+        out["solvers"][solver] = {"runs": runs, "ms_per_run": statistics.mean(r["ms"] for r in runs),
+                                  "kernels_after_solve": kern}
+    out["peak_gbs"] = peak
+    out["peak_kind"] = peak_kind
+    if not args.no_cpu:
+        oracle = load_oracle()
+        oracle.build()
+        threads = os.cpu_count() or 1
+        s = oracle.parse_deck(config2_deck(n, "cg"))
+        ch = oracle.OracleChunk(s, oracle.make_opts(mode=oracle.MODE_TEALEAF, order=oracle.ORDER_THREADS,
+                                                    nthreads=threads))
+        ch.initialise()
+        t = {}
+        for cap in (5, 25):
+            s.maxiters = cap
+            ch.halo(1, ["energy", "density"])
+            t0 = time.perf_counter()
+            ch.solve(s.dtinit / s.dx ** 2, s.dtinit / s.dy ** 2)
+            t[cap] = time.perf_counter() - t0
+        per_iter = (t[25] - t[5]) / 20
+        cg_iters = sum(out["solvers"]["cg"]["runs"][0]["iters"])
+        out["cpu_cg"] = {"ms_per_iteration": per_iter * 1e3, "cores": threads, "kind": "port",
+                         "estimated_ms_per_run": per_iter * 1e3 * cg_iters}
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -388,10 +474,14 @@ def main():
     ap.add_argument("--size", type=int, default=8192)
     ap.add_argument("--variant", default="all", choices=["all", "fp64", "fp32_ir"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="timestep", choices=["timestep", "config2"],
+                    help="timestep: the headline line; config2: the 4096^2 CG/Cheby/PPCG suite")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
-    if args.impl == "reference":
+    if args.workload == "config2":
+        run_config2(args)
+    elif args.impl == "reference":
         reference_arm(args)
     else:
         gpu_arm(args)

@@ -173,8 +173,10 @@ int tl_timer_stop(tl_ctx *ctx, double *ms);
 
 /* Times `reps` back-to-back launches of one fused iteration kernel (0: the CG
  * p-update + stencil + p.w step, 1: the u/r update + r.r step, 2: the FP32
- * stencil step, 3: the FP32 update step) on the current fields; for roofline
- * measurements. */
+ * stencil step, 3: the FP32 update step, 4: the Chebyshev step, 5: a PPCG
+ * inner sweep) on the current fields; for roofline measurements.  The
+ * launches overwrite solver work fields (p, w, r, u, sd and their second
+ * buffers): call it after the solves whose fields matter. */
 int tl_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch);
 
 /* Field summary {vol, mass, ie, temp} of caller-owned device arrays, with no

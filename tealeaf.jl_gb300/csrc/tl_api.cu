@@ -384,14 +384,20 @@ extern "C" int tl_timer_stop(tl_ctx *ctx, double *ms) {
 extern "C" int tl_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch) {
   if (!ctx || !ms_per_launch || reps < 1 || ctx->cfg.mode != TL_MODE_TEALEAF) return TL_ERR_ARG;
   const Fields &F = ctx->F;
-  if (kernel >= 2) return tl_ir_bench_kernel(ctx, kernel, reps, ms_per_launch);
-  if (kernel < 0) return TL_ERR_ARG;
+  if (kernel == 2 || kernel == 3) return tl_ir_bench_kernel(ctx, kernel, reps, ms_per_launch);
+  if (kernel < 0 || kernel > 5) return TL_ERR_ARG;
   launch_init_diag(ctx->stream, F, ctx->g);
   CKL();
   CK(cudaEventRecord(ctx->tev0, ctx->stream));
   for (int k = 0; k < reps; ++k) {
     if (kernel == 0) launch_tl_w(ctx->stream, F, ctx->g, ctx->walk_w64, (k & 1) ? F.pb : F.p, (k & 1) ? F.p : F.pb, 0, 0);
-    else launch_tl_ur(ctx->stream, F, ctx->g, ctx->walk_ur64, F.pb, 0, 0, 0, 0);
+    else if (kernel == 1) launch_tl_ur(ctx->stream, F, ctx->g, ctx->walk_ur64, F.pb, 0, 0, 0, 0);
+    else if (kernel == 4)
+      launch_cheby_step(ctx->stream, F, ctx->g, ctx->walk_w64, (k & 1) ? F.ub : F.u, (k & 1) ? F.u : F.ub, 0, 0, 0, 0,
+                        0);
+    else
+      launch_ppcg_inner(ctx->stream, F, ctx->g, ctx->walk_w64, (k & 1) ? F.sdb : F.sd, (k & 1) ? F.sd : F.sdb, 1, 0, 0,
+                        0, 0, 0);
   }
   CKL();
   CK(cudaEventRecord(ctx->tev1, ctx->stream));

@@ -54,7 +54,8 @@ struct OpCheby {
   }
   __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
     const int k = F.sc->cheby_iters + 1;  // this step's chebyiters (Cheby.jl:35)
-    const double ca = F.chebyalpha[k + 1], cb = F.chebybeta[k + 1];
+    const int idx = min(k + 1, F.sc->maxiters + 1);  // the tables hold maxiters + 2 entries
+    const double ca = F.chebyalpha[idx], cb = F.chebybeta[idx];
     SrcField src;
     src.f = usrc;
     march<!EXACT>(g, F.kx, F.ky, F.diag, src, i0, j0, j1,
