@@ -179,6 +179,20 @@ int tl_timer_stop(tl_ctx *ctx, double *ms);
  * buffers): call it after the solves whose fields matter. */
 int tl_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch);
 
+/* Many independent decks (tealeaf-mode contexts of any sizes on the current
+ * device) solved by the fused FP64 CG in one graph launch: the persistent
+ * blocks are shared over the decks in proportion to their cells, a converged
+ * deck drops out (per-deck convergence mask) and its blocks go to the decks
+ * still running.  Each deck's solve is CG.solve! (src/solvers/CG.jl:7-29)
+ * with that deck's rx[k], ry[k]; results[k] is the deck's result.  The batch
+ * borrows the contexts: destroy it before them. */
+typedef struct tl_batch tl_batch;
+int tl_batch_create(tl_batch **out, tl_ctx *const *ctxs, int n);
+int tl_batch_destroy(tl_batch *batch);
+const char *tl_batch_last_error(const tl_batch *batch);
+int tl_batch_solve(tl_batch *batch, const double *rx, const double *ry, const tl_params *params, tl_result *results);
+int tl_batch_last_ms(tl_batch *batch, double *ms);  /* device time of the last batched iteration loop */
+
 /* Field summary {vol, mass, ie, temp} of caller-owned device arrays, with no
  * device allocation by the library.  No counterpart in the reference: it is
  * for callers that cannot let a library call cudaMalloc, such as a host

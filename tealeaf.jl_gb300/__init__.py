@@ -286,6 +286,75 @@ def diffuse(chunk: Chunk, settings: Settings, problemfile: Optional[str] = None)
     return steps, summaries
 
 
+class Batch:
+    """Many independent decks (tealeaf-mode Chunks of any sizes) whose CG
+    solves run together in one graph launch (tl_batch_*)."""
+
+    def __init__(self, chunks):
+        self.lib = _abi.load()
+        self.chunks = list(chunks)
+        arr = (C.c_void_p * len(self.chunks))(*[c.ctx.value for c in self.chunks])
+        self._b = C.c_void_p()
+        rc = self.lib.tl_batch_create(C.byref(self._b), arr, len(self.chunks))
+        if rc:
+            msg = self.lib.tl_batch_last_error(self._b).decode()
+            self.lib.tl_batch_destroy(self._b)
+            self._b = None
+            raise TeaLeafError(rc, msg)
+
+    def close(self):
+        if getattr(self, "_b", None):
+            self.lib.tl_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        self.close()
+
+    def solve(self, settings_list) -> List[SolveResult]:
+        """CG.solve!(chunk, set, rx, ry) for every deck at once; the solver
+        parameters (eps, maxiters, coefficient, criterion) come from the first
+        deck's settings, rx/ry from each deck's own."""
+        n = len(self.chunks)
+        rx = (C.c_double * n)(*[s.dtinit / s.dx ** 2 for s in settings_list])
+        ry = (C.c_double * n)(*[s.dtinit / s.dy ** 2 for s in settings_list])
+        prm = _params(settings_list[0], _abi.SOLVER_CG)
+        prm.exact = 0
+        prm.precision = _abi.PREC_FP64
+        res = (_abi.Result * n)()
+        rc = self.lib.tl_batch_solve(self._b, rx, ry, C.byref(prm), res)
+        if rc:
+            raise TeaLeafError(rc, self.lib.tl_batch_last_error(self._b).decode())
+        ms = C.c_double()
+        self.lib.tl_batch_last_ms(self._b, C.byref(ms))
+        out = []
+        for k, s in enumerate(settings_list):
+            s.resettoexchange()
+            s.toexchange["u"] = s.toexchange["p"] = True
+            r = res[k]
+            out.append(SolveResult(r.iters, r.cg_iters, r.inner_iters, r.est_iters, r.error, r.eigmin, r.eigmax,
+                                   bool(r.converged), r.refinements, r.rel_residual, ms.value, r.launches))
+        return out
+
+
+def diffuse_batch(chunks, settings_list, steps: Optional[int] = None):
+    """diffuse! over many decks with batched CG solves: per timestep the halo
+    of energy and density of every deck, one batched solve, solvefinished!.
+    Returns per step the list of per-deck results and the batch's loop time."""
+    batch = Batch(chunks)
+    history = []
+    try:
+        nsteps = steps if steps is not None else min(s.endstep for s in settings_list)
+        for _ in range(nsteps):
+            for c, s in zip(chunks, settings_list):
+                haloupdate(c, s, 1, ["energy", "density"])
+            history.append(batch.solve(settings_list))
+            for c, s in zip(chunks, settings_list):
+                solvefinished(c, s)
+    finally:
+        batch.close()
+    return history
+
+
 _CHUNK_DUMP_FIELDS = ["density0", "density", "energy0", "energy", "u", "u0", "p", "r", "mi", "w", "kx", "ky",
                       "sd"]
 

@@ -73,6 +73,11 @@ SIGNATURES = {
     "tl_timer_start": ([_CTX], C.c_int),
     "tl_timer_stop": ([_CTX, _P(C.c_double)], C.c_int),
     "tl_bench_kernel": ([_CTX, C.c_int, C.c_int, _P(C.c_double)], C.c_int),
+    "tl_batch_create": ([_P(C.c_void_p), _P(C.c_void_p), C.c_int], C.c_int),
+    "tl_batch_destroy": ([C.c_void_p], C.c_int),
+    "tl_batch_last_error": ([C.c_void_p], C.c_char_p),
+    "tl_batch_solve": ([C.c_void_p, _P(C.c_double), _P(C.c_double), _P(Params), _P(Result)], C.c_int),
+    "tl_batch_last_ms": ([C.c_void_p, _P(C.c_double)], C.c_int),
     "tl_field_summary_noalloc": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
                                   C.c_longlong, C.c_void_p, C.c_void_p, C.c_char_p, C.c_int], C.c_int),
 }

@@ -1,0 +1,452 @@
+// tl_batch.cu -- many independent decks of uneven sizes solved by CG in one
+// graph launch.
+//
+// Every deck keeps its own context (fields, scalars, reduction scratch).  The
+// batch owns a device table of the decks and a block map: the persistent
+// blocks of each batched kernel are split over the unconverged decks in
+// proportion to their cells (at least one each).  A batched kernel's block
+// looks up its deck, walks that deck's tiles with the deck's share of blocks
+// and reduces into the deck's scratch; the last block of a deck runs the
+// deck's epilogue (alpha, or beta and the convergence test).  A converged
+// deck's blocks return at once (the per-deck convergence mask), and at the end
+// of every two-iteration loop body the map is rebuilt over the decks still
+// running, which also sets the while-node's condition.
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "tl_cg_ops.cuh"
+#include "tl_solvers.h"
+
+namespace tl {
+namespace {
+
+constexpr int BATCH_MAX = 1024;  // decks per batch
+constexpr int BATCH_WARPS = 8;
+constexpr int BATCH_ROWS = 8;
+
+struct DeckDesc {
+  Fields F;
+  Geom g;
+  int ntx, tiles;
+  long long cells;
+};
+
+struct BatchMap {
+  int n;
+  int active;
+  int total_w, total_u;     // blocks of the W and UR launches
+  int first_w[BATCH_MAX + 1], nblk_w[BATCH_MAX];
+  int first_u[BATCH_MAX + 1], nblk_u[BATCH_MAX];
+};
+
+__device__ __forceinline__ int find_deck(const int *first, const int *nblk, int n, int b) {
+  int lo = 0, hi = n - 1, d = -1;
+  while (lo <= hi) {  // last deck whose first block is <= b
+    const int mid = (lo + hi) >> 1;
+    if (first[mid] <= b) {
+      d = mid;
+      lo = mid + 1;
+    } else {
+      hi = mid - 1;
+    }
+  }
+  if (d >= 0 && b < first[d] + nblk[d]) return d;
+  return -1;
+}
+
+// The deterministic tree of tl_walk.cuh, over a deck's own blocks.
+template <int N, class Op>
+__device__ __forceinline__ void finish_deck(double (&acc)[N], const Op &op, int nblocks, int lb) {
+  __shared__ double ws[N][32];
+  __shared__ int is_last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double *partials = op.F.partials;
+  unsigned *counter = op.F.counter;
+#pragma unroll
+  for (int a = 0; a < N; ++a) {
+    const double v = warp_butterfly(acc[a]);
+    if (lane == 0) ws[a][warp] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int a = 0; a < N; ++a) {
+      double b = ws[a][0];
+      for (int w = 1; w < nw; ++w) b = dadd(b, ws[a][w]);
+      partials[(size_t)a * nblocks + lb] = b;
+    }
+    __threadfence();
+    is_last = (atomicAdd(counter, 1u) == (unsigned)nblocks - 1);
+  }
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+#pragma unroll
+  for (int a = 0; a < N; ++a) {
+    double v = 0.0;
+    for (int k = threadIdx.x; k < nblocks; k += blockDim.x) v = dadd(v, __ldcg(partials + (size_t)a * nblocks + k));
+    v = warp_butterfly(v);
+    if (lane == 0) ws[a][warp] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot[N];
+#pragma unroll
+    for (int a = 0; a < N; ++a) {
+      tot[a] = ws[a][0];
+      for (int w = 1; w < nw; ++w) tot[a] = dadd(tot[a], ws[a][w]);
+    }
+    *counter = 0u;
+    op.fin(tot);
+  }
+}
+
+template <class Op>
+__device__ __forceinline__ void walk_deck(const DeckDesc &D, const Op &op, int lb, int nblocks, double (&acc)[1]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int TW = 64 * BATCH_WARPS;
+  for (int t = lb; t < D.tiles; t += nblocks) {
+    const int tx = t % D.ntx, ty = t / D.ntx;
+    const int i0 = tx * TW + warp * 64 + 2 * lane;
+    const int j0 = ty * BATCH_ROWS;
+    const int j1 = min(j0 + BATCH_ROWS, D.g.ny);
+    op.tile(i0, j0, j1, acc);
+  }
+}
+
+// W step of every unconverged deck: p' = beta p + r, w = A p', p'.w.
+__global__ void __launch_bounds__(256) k_batch_w(const DeckDesc *decks, const BatchMap *map, int parity) {
+  const int d = find_deck(map->first_w, map->nblk_w, map->n, blockIdx.x);
+  if (d < 0) return;
+  const DeckDesc &D = decks[d];
+  if (D.F.sc->done) return;  // the deck's convergence mask: uniform over its blocks
+  OpTlW<false> op;
+  op.F = D.F;
+  op.g = D.g;
+  op.psrc = parity ? D.F.pb : D.F.p;
+  op.pdst = parity ? D.F.p : D.F.pb;
+  op.guard = 0;
+  op.store_coef = 1;
+  double acc[1] = {0.0};
+  const int lb = blockIdx.x - map->first_w[d], nb = map->nblk_w[d];
+  walk_deck(D, op, lb, nb, acc);
+  finish_deck<1>(acc, op, nb, lb);
+}
+
+// UR step of every unconverged deck: u += alpha p', r -= alpha w, r.r, then
+// the deck's beta and convergence test.
+__global__ void __launch_bounds__(256) k_batch_ur(const DeckDesc *decks, const BatchMap *map, int parity) {
+  const int d = find_deck(map->first_u, map->nblk_u, map->n, blockIdx.x);
+  if (d < 0) return;
+  const DeckDesc &D = decks[d];
+  if (D.F.sc->done) return;
+  OpTlUR<false> op;
+  op.F = D.F;
+  op.g = D.g;
+  op.p = parity ? D.F.p : D.F.pb;
+  op.guard = 0;
+  op.cond = 0;
+  op.set_cond = 0;
+  double acc[1] = {0.0};
+  const int lb = blockIdx.x - map->first_u[d], nb = map->nblk_u[d];
+  walk_deck(D, op, lb, nb, acc);
+  finish_deck<1>(acc, op, nb, lb);
+}
+
+// Shares `total` blocks over the unconverged decks in proportion to their
+// cells: one each, the rest in proportion (rounded down), at most one block
+// per tile.
+__device__ void share(const DeckDesc *decks, BatchMap *map, const int *act, int total, int *first, int *nblk) {
+  __shared__ long long cells_sum;
+  __shared__ int spare;
+  const int n = map->n;
+  if (threadIdx.x == 0) {
+    long long s = 0;
+    int na = 0;
+    for (int d = 0; d < n; ++d)
+      if (act[d]) {
+        s += decks[d].cells;
+        ++na;
+      }
+    cells_sum = s;
+    spare = total - na;
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < n; d += blockDim.x) {
+    int b = 0;
+    if (act[d]) {
+      const double want = cells_sum > 0 ? (double)spare * (double)decks[d].cells / (double)cells_sum : 0.0;
+      b = 1 + (int)want;
+      if (b > decks[d].tiles) b = decks[d].tiles;
+    }
+    nblk[d] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int f = 0;
+    for (int d = 0; d < n; ++d) {
+      first[d] = f;
+      f += nblk[d];
+    }
+    first[n] = f;
+  }
+  __syncthreads();
+}
+
+// Rebuilds the block map over the decks still running and sets the loop
+// condition (any deck left).
+__global__ void k_batch_map(const DeckDesc *decks, BatchMap *map, cudaGraphConditionalHandle cond, int set_cond) {
+  __shared__ int act[BATCH_MAX];
+  __shared__ int nact;
+  const int n = map->n;
+  if (threadIdx.x == 0) nact = 0;
+  __syncthreads();
+  for (int d = threadIdx.x; d < n; d += blockDim.x) {
+    act[d] = decks[d].F.sc->done ? 0 : 1;
+    if (act[d]) atomicAdd(&nact, 1);
+  }
+  __syncthreads();
+  share(decks, map, act, map->total_w, map->first_w, map->nblk_w);
+  share(decks, map, act, map->total_u, map->first_u, map->nblk_u);
+  if (threadIdx.x == 0) {
+    map->active = nact;
+    if (set_cond) cudaGraphSetConditional(cond, nact > 0 ? 1u : 0u);
+  }
+}
+
+}  // namespace
+}  // namespace tl
+
+using namespace tl;
+
+struct tl_batch {
+  std::vector<tl_ctx *> ctx;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  DeckDesc *d_decks = nullptr;
+  BatchMap *d_map = nullptr;
+  BatchMap *h_map = nullptr;
+  int total_w = 0, total_u = 0;
+  cudaGraphExec_t graph = nullptr;
+  double last_ms = 0.0;
+  char msg[512] = {};
+};
+
+namespace {
+
+int bfail(tl_batch *b, cudaError_t e, const char *what) {
+  snprintf(b->msg, sizeof b->msg, "CUDA error in %s: %s", what, cudaGetErrorString(e));
+  return TL_ERR_CUDA;
+}
+#define BCK(x)                                  \
+  do {                                          \
+    cudaError_t e_ = (x);                       \
+    if (e_ != cudaSuccess) return bfail(b, e_, #x); \
+  } while (0)
+
+int build_graph(tl_batch *b) {
+  cudaGraph_t graph = nullptr;
+  BCK(cudaGraphCreate(&graph, 0));
+  cudaGraphConditionalHandle h;
+  cudaError_t e = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return bfail(b, e, "cudaGraphConditionalHandleCreate");
+  }
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return bfail(b, e, "cudaGraphAddNode(while)");
+  }
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  e = cudaStreamBeginCaptureToGraph(b->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return bfail(b, e, "cudaStreamBeginCaptureToGraph");
+  }
+  for (int parity = 0; parity < 2; ++parity) {
+    k_batch_w<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
+    k_batch_ur<<<b->total_u, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
+  }
+  k_batch_map<<<1, 256, 0, b->stream>>>(b->d_decks, b->d_map, h, 1);
+  cudaError_t le = cudaGetLastError();
+  cudaGraph_t captured = nullptr;
+  e = cudaStreamEndCapture(b->stream, &captured);
+  if (e != cudaSuccess || le != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return bfail(b, e != cudaSuccess ? e : le, "capture of the batch loop");
+  }
+  e = cudaGraphInstantiate(&b->graph, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return bfail(b, e, "cudaGraphInstantiate");
+  return TL_OK;
+}
+
+}  // namespace
+
+extern "C" int tl_batch_create(tl_batch **out, tl_ctx *const *ctxs, int n) {
+  if (!out) return TL_ERR_ARG;
+  *out = nullptr;
+  tl_batch *b = new (std::nothrow) tl_batch();
+  if (!b) return TL_ERR_NOMEM;
+  *out = b;
+  if (!ctxs || n < 1 || n > BATCH_MAX) {
+    snprintf(b->msg, sizeof b->msg, "batch of %d decks outside 1..%d", n, BATCH_MAX);
+    return TL_ERR_ARG;
+  }
+  BCK(cudaGetDevice(&b->device));
+  int sms = 0;
+  BCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
+  std::vector<DeckDesc> h(n);
+  for (int k = 0; k < n; ++k) {
+    tl_ctx *c = ctxs[k];
+    if (!c || c->cfg.mode != TL_MODE_TEALEAF || c->device != b->device) {
+      snprintf(b->msg, sizeof b->msg, "deck %d: needs a tealeaf-mode context on the current device", k);
+      return TL_ERR_ARG;
+    }
+    b->ctx.push_back(c);
+    h[k].F = c->F;
+    h[k].g = c->g;
+    h[k].ntx = (c->g.nx + 64 * BATCH_WARPS - 1) / (64 * BATCH_WARPS);
+    h[k].tiles = h[k].ntx * ((c->g.ny + BATCH_ROWS - 1) / BATCH_ROWS);
+    h[k].cells = (long long)c->g.nx * c->g.ny;
+  }
+  // blocks: the occupancy of each batched kernel at 256 threads, at least one per deck
+  int occ_w = 0, occ_u = 0;
+  BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_w, k_batch_w, 256, 0));
+  BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_u, k_batch_ur, 256, 0));
+  b->total_w = (occ_w > 0 ? occ_w : 1) * sms;
+  b->total_u = (occ_u > 0 ? occ_u : 1) * sms;
+  const int maxb = ctxs[0]->max_blocks;
+  for (int k = 0; k < n; ++k)
+    if (ctxs[k]->max_blocks < maxb) {
+      snprintf(b->msg, sizeof b->msg, "deck %d: reduction scratch smaller than the batch's share", k);
+      return TL_ERR_ARG;
+    }
+  if (b->total_w > maxb) b->total_w = maxb;
+  if (b->total_u > maxb) b->total_u = maxb;
+  if (b->total_w < n) b->total_w = n;
+  if (b->total_u < n) b->total_u = n;
+  BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  BCK(cudaEventCreate(&b->ev0));
+  BCK(cudaEventCreate(&b->ev1));
+  BCK(cudaMalloc(&b->d_decks, sizeof(DeckDesc) * n));
+  BCK(cudaMalloc(&b->d_map, sizeof(BatchMap)));
+  BCK(cudaMallocHost(&b->h_map, sizeof(BatchMap)));
+  memset(b->h_map, 0, sizeof(BatchMap));
+  b->h_map->n = n;
+  b->h_map->total_w = b->total_w;
+  b->h_map->total_u = b->total_u;
+  BCK(cudaMemcpyAsync(b->d_decks, h.data(), sizeof(DeckDesc) * n, cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaMemcpyAsync(b->d_map, b->h_map, sizeof(BatchMap), cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  return TL_OK;
+}
+
+extern "C" int tl_batch_destroy(tl_batch *b) {
+  if (!b) return TL_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->d_decks) cudaFree(b->d_decks);
+  if (b->d_map) cudaFree(b->d_map);
+  if (b->h_map) cudaFreeHost(b->h_map);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return TL_OK;
+}
+
+extern "C" const char *tl_batch_last_error(const tl_batch *b) { return b ? b->msg : "null batch"; }
+
+extern "C" int tl_batch_solve(tl_batch *b, const double *rx, const double *ry, const tl_params *prm,
+                              tl_result *results) {
+  if (!b || !rx || !ry || !prm || !results) return TL_ERR_ARG;
+  if (prm->solver != TL_SOLVER_CG || prm->precision != TL_PREC_FP64 || prm->exact) {
+    snprintf(b->msg, sizeof b->msg, "batched solves run the fused FP64 CG (solver CG, FP64, exact 0)");
+    return TL_ERR_ARG;
+  }
+  const int n = (int)b->ctx.size();
+  // each deck's CG.init!, halo of u, p and copyu, on the batch stream
+  std::vector<cudaStream_t> own(n);
+  for (int k = 0; k < n; ++k) {
+    tl_ctx *ctx = b->ctx[k];
+    if (!ctx->initialised || prm->maxiters > ctx->cfg.maxiters) {
+      snprintf(b->msg, sizeof b->msg, "deck %d: not initialised, or maxiters beyond its tables", k);
+      return TL_ERR_STATE;
+    }
+    own[k] = ctx->stream;
+    ctx->stream = b->stream;
+  }
+  auto restore = [&]() {
+    for (int k = 0; k < n; ++k) b->ctx[k]->stream = own[k];
+  };
+  int rc = TL_OK;
+  for (int k = 0; k < n && !rc; ++k) {
+    tl_ctx *ctx = b->ctx[k];
+    memset(&results[k], 0, sizeof(tl_result));
+    ctx->launches = 0;
+    rc = tl_cg_init(ctx, rx[k], ry[k], prm->coefficient, 0);
+    if (!rc) rc = tl_set_loop_params(ctx, prm, 0, 0);
+    const int up[2] = {TL_EX_U, TL_EX_P};
+    if (!rc) rc = tl_halo_update(ctx, 1, up, 2, 1);
+    if (!rc) rc = tl_copy_u(ctx);
+    if (rc) snprintf(b->msg, sizeof b->msg, "deck %d: %s", k, ctx->msg);
+  }
+  if (rc) {
+    restore();
+    return rc;
+  }
+  if (prm->maxiters >= 1) {
+    k_batch_map<<<1, 256, 0, b->stream>>>(b->d_decks, b->d_map, 0, 0);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && !b->graph) rc = build_graph(b);
+    if (e == cudaSuccess && !rc) e = cudaEventRecord(b->ev0, b->stream);
+    if (e == cudaSuccess && !rc) e = cudaGraphLaunch(b->graph, b->stream);
+    if (e == cudaSuccess && !rc) e = cudaEventRecord(b->ev1, b->stream);
+    if (e == cudaSuccess && !rc) e = cudaEventSynchronize(b->ev1);
+    float ms = 0.f;
+    if (e == cudaSuccess && !rc) e = cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+    b->last_ms = ms;
+    if (e != cudaSuccess) rc = bfail(b, e, "batch loop");
+  }
+  // per deck: the last iteration's p! and the halo of u, p; the results
+  for (int k = 0; k < n && !rc; ++k) {
+    tl_ctx *ctx = b->ctx[k];
+    rc = tl_read_scalars(ctx);
+    if (rc) break;
+    const DevScalars &sc = *ctx->host_sc;
+    if (prm->maxiters >= 1) {
+      const double *pcur = (sc.iter & 1) ? ctx->F.pb : ctx->F.p;
+      launch_tl_p(ctx->stream, ctx->F, ctx->g, ctx->walk_ur64, pcur, ctx->F.p, 0);
+      rc = tl_halo_update(ctx, 1, nullptr, -1, 1);
+    }
+    results[k].iters = sc.iter;
+    results[k].cg_iters = sc.iter;
+    results[k].error = prm->maxiters >= 1 ? sc.error : ERROR_START;
+    results[k].converged = sc.converged;
+    results[k].rel_residual = -1.0;
+    results[k].launches = 0;
+  }
+  if (!rc) {
+    cudaError_t e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) rc = bfail(b, e, "batch epilogue");
+  }
+  restore();
+  return rc;
+}
+
+extern "C" int tl_batch_last_ms(tl_batch *b, double *ms) {
+  if (!b || !ms) return TL_ERR_ARG;
+  *ms = b->last_ms;
+  return TL_OK;
+}
