@@ -465,6 +465,64 @@ def run_config2(args):
     print(json.dumps(out))
 
 
+def config4_decks(count: int = 128, seed: int = DECK_SEED + 4):
+    """Seeded random-rectangle decks with nx, ny drawn from 256..2048 in steps of 128."""
+    rng = np.random.default_rng(seed)
+    sizes = [(int(rng.integers(2, 17)) * 128, int(rng.integers(2, 17)) * 128) for _ in range(count)]
+    texts = []
+    for k, (nx, ny) in enumerate(sizes):
+        t = make_deck(nx, seed=seed * 1000 + k, steps=10, maxiters=40000)
+        texts.append(t.replace(f"y_cells={nx}", f"y_cells={ny}"))
+    return sizes, texts
+
+
+def run_config4(args):
+    """128 independent decks of uneven sizes, 10 timesteps each, CG to 1e-10
+    relative residual: one batched graph launch per timestep against the same
+    decks solved one after another by the single-deck fused CG."""
+    import torch
+    torch.cuda.set_device(0)
+    tl = load_package()
+    sizes, texts = config4_decks(args.decks)
+    steps = 10
+    out = {"workload": f"config4: {len(texts)} random-rectangle decks, nx, ny in 256..2048 step 128, {steps} steps, "
+                       "CG to 1e-10 relative (recursive residual)", "cells": sum(a * b for a, b in sizes)}
+    for mode in ("batched", "sequential"):
+        sets = [tl.Settings.from_text(t, mode=1, criterion=1) for t in texts]
+        chunks = [tl.initialiseapp(s) for s in sets]
+        lib = chunks[0].lib
+        for c in chunks:
+            c.check(lib.tl_synchronize(c.ctx))
+        t0 = time.perf_counter()
+        iters = 0
+        if mode == "batched":
+            batch = tl.Batch(chunks)
+            for _ in range(steps):
+                for c, s in zip(chunks, sets):
+                    tl.haloupdate(c, s, 1, ["energy", "density"])
+                res = batch.solve(sets)
+                iters += sum(r.iters for r in res)
+                for c, s in zip(chunks, sets):
+                    tl.solvefinished(c, s)
+            batch.close()
+        else:
+            for c, s in zip(chunks, sets):
+                for _ in range(steps):
+                    tl.haloupdate(c, s, 1, ["energy", "density"])
+                    r = tl.CG.solve(c, s, s.dtinit / s.dx ** 2, s.dtinit / s.dy ** 2)
+                    iters += r.iters
+                    tl.solvefinished(c, s)
+        for c in chunks:
+            c.check(lib.tl_synchronize(c.ctx))
+        wall = time.perf_counter() - t0
+        summ = [tl.fieldsummary(c, s, problemfile=None)[3] for c, s in zip(chunks, sets)]
+        out[mode] = {"seconds": wall, "iterations": iters, "temp_summaries_first4": summ[:4]}
+        for c in chunks:
+            c.close()
+    out["speedup"] = out["sequential"]["seconds"] / out["batched"]["seconds"]
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -474,13 +532,17 @@ def main():
     ap.add_argument("--size", type=int, default=8192)
     ap.add_argument("--variant", default="all", choices=["all", "fp64", "fp32_ir"])
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="timestep", choices=["timestep", "config2"],
-                    help="timestep: the headline line; config2: the 4096^2 CG/Cheby/PPCG suite")
+    ap.add_argument("--workload", default="timestep", choices=["timestep", "config2", "config4"],
+                    help="timestep: the headline line; config2: the 4096^2 CG/Cheby/PPCG suite; "
+                         "config4: 128 uneven decks, batched against sequential")
+    ap.add_argument("--decks", type=int, default=128)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
     if args.workload == "config2":
         run_config2(args)
+    elif args.workload == "config4":
+        run_config4(args)
     elif args.impl == "reference":
         reference_arm(args)
     else:

@@ -141,6 +141,15 @@ int tl_solve_finished(tl_ctx *ctx, int checkresult);
  * interior; temp is the reference's quantity, the other three are added. */
 int tl_field_summary(tl_ctx *ctx, double out[4]);
 
+/* diffuse! (src/TeaLeaf.jl:62-83) inside the library: for each of `nsteps`
+ * timesteps, rx = dt/dx^2, ry = dt/dy^2, the halo of energy and density, the
+ * solve, solvefinished!, and the field summary every `summaryfrequency`
+ * steps and after the last.  results[nsteps]; summaries[4 * n] receives up
+ * to `maxsummaries` summaries, *nsummaries how many were taken (checkresult
+ * 0 takes none, like fieldsummary). */
+int tl_diffuse(tl_ctx *ctx, const tl_params *params, double dt, int nsteps, int summaryfrequency, int checkresult,
+               tl_result *results, double *summaries, int maxsummaries, int *nsummaries);
+
 /* copyu! (src/kernels.jl:217-220), residual! (:227-232), finalise! (:239-242) */
 int tl_copy_u(tl_ctx *ctx);
 int tl_residual(tl_ctx *ctx);

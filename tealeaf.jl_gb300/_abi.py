@@ -73,6 +73,8 @@ SIGNATURES = {
     "tl_timer_start": ([_CTX], C.c_int),
     "tl_timer_stop": ([_CTX, _P(C.c_double)], C.c_int),
     "tl_bench_kernel": ([_CTX, C.c_int, C.c_int, _P(C.c_double)], C.c_int),
+    "tl_diffuse": ([_CTX, _P(Params), C.c_double, C.c_int, C.c_int, C.c_int, _P(Result), _P(C.c_double), C.c_int,
+                    _P(C.c_int)], C.c_int),
     "tl_batch_create": ([_P(C.c_void_p), _P(C.c_void_p), C.c_int], C.c_int),
     "tl_batch_destroy": ([C.c_void_p], C.c_int),
     "tl_batch_last_error": ([C.c_void_p], C.c_char_p),

@@ -454,3 +454,33 @@ extern "C" int tl_set_layout(tl_ctx *ctx, int kernel, int warps, int rows, int b
   tl_release_ir_graphs(ctx);
   return TL_OK;
 }
+
+extern "C" int tl_diffuse(tl_ctx *ctx, const tl_params *prm, double dt, int nsteps, int summaryfrequency,
+                          int checkresult, tl_result *results, double *summaries, int maxsummaries,
+                          int *nsummaries) {
+  if (!ctx || !prm || !results || nsteps < 0 || summaryfrequency < 1) return TL_ERR_ARG;
+  if (nsummaries) *nsummaries = 0;
+  const double rx = dt / (ctx->cfg.dx * ctx->cfg.dx);  // TeaLeaf.jl:69-70
+  const double ry = dt / (ctx->cfg.dy * ctx->cfg.dy);
+  int taken = 0, rc;
+  auto summary = [&]() -> int {
+    if (!checkresult) return TL_OK;
+    double out[4];
+    int r = tl_field_summary(ctx, out);
+    if (r) return r;
+    if (summaries && taken < maxsummaries)
+      for (int k = 0; k < 4; ++k) summaries[4 * taken + k] = out[k];
+    ++taken;
+    return TL_OK;
+  };
+  for (int tt = 1; tt <= nsteps; ++tt) {
+    const int ex[2] = {TL_EX_ENERGY, TL_EX_DENSITY};
+    if ((rc = tl_halo_update(ctx, 1, ex, 2, 1))) return rc;
+    if ((rc = tl_solve(ctx, rx, ry, prm, &results[tt - 1]))) return rc;
+    if ((rc = tl_solve_finished(ctx, checkresult))) return rc;
+    if (tt % summaryfrequency == 0 && (rc = summary())) return rc;
+  }
+  if ((rc = summary())) return rc;
+  if (nsummaries) *nsummaries = taken < maxsummaries ? taken : maxsummaries;
+  return TL_OK;
+}

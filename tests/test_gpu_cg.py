@@ -110,6 +110,28 @@ def test_halo_both_modes(tl, built_lib):
         np.testing.assert_array_equal(chunk.field("sd"), och.field("sd"))
 
 
+@pytest.mark.parametrize("mode", [REF, TEA])
+def test_native_diffuse_matches_host_driver(tl, built_lib, mode):
+    """tl_diffuse (the timestep loop inside the library) against the host
+    mirror's diffuse, which calls the same entry points one by one."""
+    import ctypes as C
+    s1 = tl.Settings.from_text(CONFIG1, mode=mode, exact=True)
+    c1 = tl.initialiseapp(s1)
+    steps, sums = tl.diffuse(c1, s1, problemfile=None)
+    s2 = tl.Settings.from_text(CONFIG1, mode=mode, exact=True)
+    c2 = tl.initialiseapp(s2)
+    prm = tl._params(s2, tl._abi.SOLVER_CG)
+    res = (tl._abi.Result * s2.endstep)()
+    out = (C.c_double * 8)()
+    ns = C.c_int()
+    c2.check(c2.lib.tl_diffuse(c2.ctx, C.byref(prm), s2.dtinit, s2.endstep, s2.summaryfrequency, 1, res, out, 2,
+                               C.byref(ns)))
+    assert [r.iters for r in res] == [r.iters for r in steps]
+    assert ns.value == 2 and tuple(out[4:8]) == tuple(sums[-1])
+    for f in FIELDS:
+        np.testing.assert_array_equal(c1.field(f), c2.field(f), err_msg=f)
+
+
 def test_coefficient_error(tl, built_lib):
     """An invalid coefficient raises like CG.jl:48-50."""
     s = tl.Settings.from_text(deck_text(coefficient=3), mode=TEA)
