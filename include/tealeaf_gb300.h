@@ -92,6 +92,8 @@ typedef struct {
   int precision;            /* TL_PREC_*                                     */
   int exact;                /* 1: tealeaf mode reproduces the reference's operation order with no FMA
                                contraction (bit-identical to the CPU restatement); 0: fused FMA kernels */
+  int warmstart;            /* CG in tealeaf mode: start from the warm-start network's prediction when
+                               its initial residual is below the plain start's (tl_warm_load) */
 } tl_params;
 
 typedef struct {
@@ -105,6 +107,10 @@ typedef struct {
   int refinements;          /* FP64 refinement passes (TL_PREC_FP32_IR)         */
   double rel_residual;      /* ||u0 - A u|| / ||u0|| after the solve (TL_CRIT_RELATIVE), else -1 */
   int launches;             /* kernels this solve launched (graph-body kernels counted per trip) */
+  int warm;                 /* 0: plain start (no warm start asked or no previous step), 1: the
+                               prediction was used, 2: the prediction lost to the plain start */
+  double r0_plain;          /* ||u0 - A u^n|| / ||u0|| of the plain start (warm start asked), else -1 */
+  double r0_pred;           /* the same for the prediction, -1 when none was made */
 } tl_result;
 
 /* Creation.  Replaces Chunk(set) (src/chunk.jl:68-89): allocates every field
@@ -225,6 +231,65 @@ int tl_batch_last_ms(tl_batch *batch, double *ms);  /* device time of the last b
 int tl_field_summary_noalloc(const double *volume, const double *density, const double *energy, const double *u,
                              int xcells, int ycells, int halodepth, long long pitch, double *out, void *stream,
                              char *err, int errlen);
+
+/* ---- learned warm start ------------------------------------------------
+ * No counterpart in the reference.  A 6-layer 3x3 convolutional network (32
+ * channels, GELU between layers, BF16 weights, FP32 accumulation on the
+ * tensor cores) reads, per cell, u^n / rms(u^n), log(rx / density) / 4 and
+ * (u^n - u^{n-1}) / rms(u^n - u^{n-1}) and returns a factor g; the predicted
+ * solution is u^n + (1 + g) (u^n - u^{n-1}).  CG starts from it only when its
+ * residual ||u^n - A x|| is below the plain start's; it must still meet eps on
+ * the true residual.
+ *
+ * Parameter vector (FP32, TL_WARM_NPARAMS values), layer by layer:
+ * W[cout][9][cin] then b[cout], with (cin, cout) = (16, 32), (32, 32) x 4,
+ * (32, 16); input channels 3..15 and output channels 1..15 are padding. */
+#define TL_WARM_NPARAMS (32 * 9 * 16 + 32 + 4 * (32 * 9 * 32 + 32) + 16 * 9 * 32 + 16)
+
+/* Loads the network into the context (copies; the weights are rounded to BF16). */
+int tl_warm_load(tl_ctx *ctx, const float *params, int nparams);
+/* Forgets the previous step (the next warm-start solve makes no prediction). */
+int tl_warm_reset(tl_ctx *ctx);
+
+/* Building blocks of training (device pointers, asynchronous on `stream`). */
+/* A crop of a deck's fields for the feature and loss kernels: pointers to
+ * cell (0, 0) of the interior, `pitch` doubles between rows, crop origin
+ * (ox, oy) of size given per call, inside the nx x ny domain. */
+typedef struct {
+  const double *u, *uprev, *rho;
+  long long pitch;
+  int nx, ny, ox, oy;
+  double rx, ry;
+  double inv_su, inv_sd;    /* 1 / rms(u), 1 / rms(u - uprev) over the domain */
+} tl_warm_crop;
+
+/* y = conv3x3(x, w) + b over N images of H x W (NHWC BF16, zero padding);
+ * mode 0: out = y; 1: out = GELU(y) and z = y (z may be NULL); 2: out = y *
+ * GELU'(gz) (input gradient through the previous layer's GELU; b may be NULL).
+ * out32 (may be NULL) receives channel 0 of y in FP32.  (cin, cout) in
+ * {(16, 32), (32, 32), (32, 16)}. */
+int tl_conv3x3_forward(const void *x, const void *w, const float *bias, const void *gz, void *z, void *out,
+                       float *out32, int N, int H, int W, int cin, int cout, int mode, void *stream);
+/* dw[cout][9][cin], then db[cout] = the weight and bias gradients; partials
+ * holds nparts * (cout*9*cin + cout) floats. */
+int tl_conv3x3_weight_grad(const void *x, const void *dz, float *partials, int nparts, float *dw, int N, int H, int W,
+                           int cin, int cout, void *stream);
+/* wt[ci][tap][co] = w[co][8 - tap][ci]: weights of the input-gradient convolution. */
+int tl_conv3x3_flip(const void *w, void *wt, int cin, int cout, void *stream);
+/* Adam (bias-corrected, step >= 1) on FP32 weights with gradient scale and
+ * elementwise clip; wbf16 (may be NULL) receives the BF16 copy. */
+int tl_adam_step(float *w, float *m, float *v, const float *grad, void *wbf16, int n, float lr, float b1, float b2,
+                 float eps, int step, float clip, float gscale, void *stream);
+/* feat[B][H][W][16] = the network input of B crops. */
+int tl_warm_features(const tl_warm_crop *crops, int B, int H, int W, void *feat, void *stream);
+/* Loss of B crops of H x W: L = mean over crops of mean((inv_sd r)^2), r =
+ * d - A((1 + g) d), over the cells at least `margin` (>= 2) from the crop
+ * edge; d = u - uprev, A the 5-point operator of the crop's deck.
+ * crop_loss[2b] = the crop's term, crop_loss[2b+1] = mean((inv_sd d)^2) (the
+ * plain start's value); dz[B][H][W][16] = dL/dg in channel 0, 0 elsewhere.
+ * resid: B*H*W doubles, sums: B*nblk*2 doubles of scratch. */
+int tl_warm_loss(const tl_warm_crop *crops, int B, int H, int W, int margin, const float *g, double *resid,
+                 double *sums, int nblk, double *crop_loss, void *dz, void *stream);
 
 #ifdef __cplusplus
 }

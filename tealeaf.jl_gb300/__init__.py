@@ -53,6 +53,9 @@ class SolveResult:
     rel_residual: float
     solve_ms: float
     launches: int
+    warm: int = 0              # 0 plain start, 1 the prediction was used, 2 it lost to the plain start
+    r0_plain: float = -1.0     # initial relative residual of the plain start (warm start asked)
+    r0_pred: float = -1.0      # the same for the prediction (-1: none made)
 
 
 class Chunk:
@@ -123,6 +126,15 @@ class Chunk:
     def set_states(self, settings: Settings):
         arr = _state_array(settings, self.mode)
         self.check(self.lib.tl_set_states(self._ctx, arr, len(settings.states)))
+
+    def warm_load(self, params: np.ndarray):
+        """Loads a warm-start network (FP32 vector of _abi.WARM_NPARAMS values)."""
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        self.check(self.lib.tl_warm_load(self._ctx, p.ctypes.data_as(C.POINTER(C.c_float)), p.size))
+
+    def warm_reset(self):
+        """Forgets the previous step: the next warm-start solve makes no prediction."""
+        self.check(self.lib.tl_warm_reset(self._ctx))
 
 
 def _state_array(settings: Settings, mode: int):
@@ -209,7 +221,7 @@ def fieldsummary(chunk: Chunk, settings: Settings, problemfile: Optional[str] = 
 def _params(settings: Settings, solver: int) -> _abi.Params:
     return _abi.Params(solver, settings.coefficient, settings.maxiters, settings.presteps,
                        settings.ppcginnersteps, int(settings.errorswitch), settings.eps, settings.epslim,
-                       settings.criterion, settings.precision, int(settings.exact))
+                       settings.criterion, settings.precision, int(settings.exact), int(settings.warmstart))
 
 
 def _solve(chunk: Chunk, settings: Settings, rx: float, ry: float, solver: int) -> SolveResult:
@@ -234,7 +246,8 @@ def _solve(chunk: Chunk, settings: Settings, rx: float, ry: float, solver: int) 
     else:
         settings.toexchange["u"] = True
     r = SolveResult(res.iters, res.cg_iters, res.inner_iters, res.est_iters, res.error, res.eigmin, res.eigmax,
-                    bool(res.converged), res.refinements, res.rel_residual, ms.value, res.launches)
+                    bool(res.converged), res.refinements, res.rel_residual, ms.value, res.launches, res.warm,
+                    res.r0_plain, res.r0_pred)
     log.info("solve complete iters=%d error=%r", r.iters, r.error)
     return r
 
@@ -386,3 +399,6 @@ def _julia_repr(v: float) -> str:
             mant += ".0"
         return f"{mant}e{int(ex)}"
     return r
+
+
+from . import warmstart  # noqa: E402  (learned warm start: network file, training, evaluation)

@@ -37,13 +37,27 @@ class State(C.Structure):
 class Params(C.Structure):
     _fields_ = [("solver", C.c_int), ("coefficient", C.c_int), ("maxiters", C.c_int), ("presteps", C.c_int),
                 ("ppcginnersteps", C.c_int), ("errorswitch", C.c_int), ("eps", C.c_double),
-                ("epslim", C.c_double), ("criterion", C.c_int), ("precision", C.c_int), ("exact", C.c_int)]
+                ("epslim", C.c_double), ("criterion", C.c_int), ("precision", C.c_int), ("exact", C.c_int),
+                ("warmstart", C.c_int)]
 
 
 class Result(C.Structure):
     _fields_ = [("iters", C.c_int), ("cg_iters", C.c_int), ("inner_iters", C.c_int), ("est_iters", C.c_int),
                 ("error", C.c_double), ("eigmin", C.c_double), ("eigmax", C.c_double), ("converged", C.c_int),
-                ("refinements", C.c_int), ("rel_residual", C.c_double), ("launches", C.c_int)]
+                ("refinements", C.c_int), ("rel_residual", C.c_double), ("launches", C.c_int), ("warm", C.c_int),
+                ("r0_plain", C.c_double), ("r0_pred", C.c_double)]
+
+
+class WarmCrop(C.Structure):
+    """tl_warm_crop: a crop of a deck's device fields for the network kernels."""
+    _fields_ = [("u", C.c_void_p), ("uprev", C.c_void_p), ("rho", C.c_void_p), ("pitch", C.c_longlong),
+                ("nx", C.c_int), ("ny", C.c_int), ("ox", C.c_int), ("oy", C.c_int), ("rx", C.c_double),
+                ("ry", C.c_double), ("inv_su", C.c_double), ("inv_sd", C.c_double)]
+
+
+# the warm-start network: (cin, cout) per layer; parameters W[cout][9][cin], b[cout]
+WARM_LAYERS = [(16, 32), (32, 32), (32, 32), (32, 32), (32, 32), (32, 16)]
+WARM_NPARAMS = sum(co * 9 * ci + co for ci, co in WARM_LAYERS)
 
 
 # every symbol the header declares, with its ctypes signature
@@ -82,6 +96,18 @@ SIGNATURES = {
     "tl_batch_last_ms": ([C.c_void_p, _P(C.c_double)], C.c_int),
     "tl_field_summary_noalloc": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
                                   C.c_longlong, C.c_void_p, C.c_void_p, C.c_char_p, C.c_int], C.c_int),
+    "tl_warm_load": ([_CTX, _P(C.c_float), C.c_int], C.c_int),
+    "tl_warm_reset": ([_CTX], C.c_int),
+    "tl_conv3x3_forward": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                            C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p], C.c_int),
+    "tl_conv3x3_weight_grad": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                C.c_int, C.c_int, C.c_void_p], C.c_int),
+    "tl_conv3x3_flip": ([C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p], C.c_int),
+    "tl_adam_step": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_float,
+                      C.c_float, C.c_float, C.c_int, C.c_float, C.c_float, C.c_void_p], C.c_int),
+    "tl_warm_features": ([C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p], C.c_int),
+    "tl_warm_loss": ([C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                      C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
 }
 
 _lib = None

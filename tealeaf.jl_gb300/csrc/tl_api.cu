@@ -152,6 +152,7 @@ extern "C" int tl_destroy(tl_ctx *ctx) {
   if (ctx->tev1) cudaEventDestroy(ctx->tev1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   tl_release_ir(ctx);
+  tl_release_warm(ctx);
   delete ctx;
   return TL_OK;
 }

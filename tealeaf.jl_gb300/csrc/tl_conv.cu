@@ -1,0 +1,514 @@
+// tl_conv.cu -- kernels of the warm-start network: 3x3 convolutions as
+// implicit GEMMs on the BF16 tensor cores (warp-level mma m16n8k16, FP32
+// accumulation) for the forward pass, the input gradient and the weight
+// gradient; feature assembly; the residual loss through the 5-point operator;
+// Adam.
+//
+// Activations are NHWC BF16 (N images of H rows x W pixels, C = 16 or 32
+// channels contiguous per pixel), zero-padded outside each image.  The three
+// input channels are padded to 16 and the one output channel to 16.  Weights
+// of a layer are [Cout][9][Cin] BF16 (tap = 3*dy + dx), biases FP32.
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstdint>
+
+#include "tl_conv.h"
+
+namespace {
+
+using bf16 = __nv_bfloat16;
+constexpr int TP = 64;  // pixels of one image row per block (4 warps x 16)
+constexpr int RB = 8;   // image rows swept by one forward block
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ void ldsm_x4_trans(uint32_t (&r)[4], const void *p) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(s));
+}
+
+__device__ __forceinline__ void ldsm_x2_trans(uint32_t (&r)[2], const void *p) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0,%1}, [%2];\n" : "=r"(r[0]), "=r"(r[1]) : "r"(s));
+}
+
+// GELU, tanh form: 0.5 z (1 + tanh(c (z + 0.044715 z^3))), c = sqrt(2/pi)
+__device__ __forceinline__ float gelu(float z) {
+  const float c = 0.7978845608028654f;
+  return 0.5f * z * (1.f + tanhf(c * (z + 0.044715f * z * z * z)));
+}
+__device__ __forceinline__ float gelu_grad(float z) {
+  const float c = 0.7978845608028654f;
+  const float t = tanhf(c * (z + 0.044715f * z * z * z));
+  return 0.5f * (1.f + t) + 0.5f * z * (1.f - t * t) * c * (1.f + 3.f * 0.044715f * z * z);
+}
+
+struct ConvArgs {
+  const bf16 *x, *w, *gz;
+  const float *bias;
+  bf16 *z, *out;
+  float *out32;
+  int N, H, W;
+};
+
+// One block: TP pixels x RB rows of one image, all COUT channels; warp w owns
+// pixels [16w, 16w+16) of the row being computed.  The weights stay in shared
+// memory for the whole sweep; the three input rows live in a ring and one new
+// row is loaded per output row.  K = 9 taps x CIN in steps of 16.
+// MODE 0: out = z; 1: out = GELU(z) (z stored when `z` is set);
+// 2: out = z * GELU'(gz) (input gradient fused with the GELU derivative).
+// `out32` (when set) receives channel 0 of z in FP32.
+template <int CIN, int COUT, int MODE>
+__global__ void __launch_bounds__(128) k_conv3x3(ConvArgs a) {
+  constexpr int PS = CIN + 8;      // pixel stride in shared memory (bf16 elements)
+  constexpr int WS = 9 * CIN + 8;  // weight row stride
+  constexpr int NT = COUT / 8;
+  constexpr int V = CIN / 8;       // 16-byte vectors per pixel
+  __shared__ __align__(16) bf16 sw[COUT][WS];
+  __shared__ __align__(16) bf16 sx[3][TP + 2][PS];
+  const int img = blockIdx.z, x0 = blockIdx.x * TP, y0 = blockIdx.y * RB;
+  const int y1 = min(a.H, y0 + RB);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g = lane >> 2, t = lane & 3, px = warp * 16;
+  const size_t plane = (size_t)a.H * a.W;
+  const bf16 *xi = a.x + (size_t)img * plane * CIN;
+
+  for (int v = tid; v < COUT * 9 * V; v += 128) {
+    const int row = v / (9 * V), c = v % (9 * V);
+    *reinterpret_cast<uint4 *>(&sw[row][c * 8]) = reinterpret_cast<const uint4 *>(a.w)[v];
+  }
+  auto load_row = [&](int yy) {
+    const int slot = (yy + 3) % 3;
+    for (int v = tid; v < (TP + 2) * V; v += 128) {
+      const int col = v / V, c8 = v % V, xx = x0 + col - 1;
+      uint4 val = make_uint4(0, 0, 0, 0);
+      if (yy >= 0 && yy < a.H && xx >= 0 && xx < a.W)
+        val = *reinterpret_cast<const uint4 *>(xi + ((size_t)yy * a.W + xx) * CIN + c8 * 8);
+      *reinterpret_cast<uint4 *>(&sx[slot][col][c8 * 8]) = val;
+    }
+  };
+  load_row(y0 - 1);
+  load_row(y0);
+  for (int y = y0; y < y1; ++y) {
+    __syncthreads();  // the previous row's reads of the slot being replaced are done
+    load_row(y + 1);
+    __syncthreads();
+    float acc[NT][4];
+#pragma unroll
+    for (int n = 0; n < NT; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
+#pragma unroll
+    for (int dy = 0; dy < 3; ++dy) {
+      const int slot = (y - 1 + dy + 3) % 3;
+#pragma unroll
+      for (int dx = 0; dx < 3; ++dx) {
+        const int tap = 3 * dy + dx;
+#pragma unroll
+        for (int cc = 0; cc < CIN; cc += 16) {
+          const bf16 *r0 = &sx[slot][px + g + dx][cc];
+          const bf16 *r8 = &sx[slot][px + g + 8 + dx][cc];
+          uint32_t af[4];
+          af[0] = *reinterpret_cast<const uint32_t *>(r0 + 2 * t);
+          af[1] = *reinterpret_cast<const uint32_t *>(r8 + 2 * t);
+          af[2] = *reinterpret_cast<const uint32_t *>(r0 + 2 * t + 8);
+          af[3] = *reinterpret_cast<const uint32_t *>(r8 + 2 * t + 8);
+#pragma unroll
+          for (int n = 0; n < NT; ++n) {
+            const bf16 *wc = &sw[n * 8 + g][tap * CIN + cc];
+            uint32_t bfr[2];
+            bfr[0] = *reinterpret_cast<const uint32_t *>(wc + 2 * t);
+            bfr[1] = *reinterpret_cast<const uint32_t *>(wc + 2 * t + 8);
+            mma_bf16(acc[n], af, bfr);
+          }
+        }
+      }
+    }
+    // rows g and g+8 of the warp's 16 pixels; channels n*8 + 2t, +1
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int xx = x0 + px + g + 8 * half;
+      if (xx >= a.W) continue;
+      const size_t pix = (size_t)img * plane + (size_t)y * a.W + xx;
+      const size_t o = pix * COUT;
+#pragma unroll
+      for (int n = 0; n < NT; ++n) {
+        const int ch = n * 8 + 2 * t;
+        float z0 = acc[n][2 * half], z1 = acc[n][2 * half + 1];
+        if (a.bias) {
+          z0 += a.bias[ch];
+          z1 += a.bias[ch + 1];
+        }
+        if (a.out32 && ch == 0) a.out32[pix] = z0;
+        float o0 = z0, o1 = z1;
+        if (MODE == 1) {
+          if (a.z) *reinterpret_cast<__nv_bfloat162 *>(a.z + o + ch) = __floats2bfloat162_rn(z0, z1);
+          o0 = gelu(z0);
+          o1 = gelu(z1);
+        } else if (MODE == 2) {
+          const __nv_bfloat162 zz = *reinterpret_cast<const __nv_bfloat162 *>(a.gz + o + ch);
+          o0 = z0 * gelu_grad(__low2float(zz));
+          o1 = z1 * gelu_grad(__high2float(zz));
+        }
+        if (a.out) *reinterpret_cast<__nv_bfloat162 *>(a.out + o + ch) = __floats2bfloat162_rn(o0, o1);
+      }
+    }
+  }
+}
+
+// Weight and bias gradients: dW[co][tap][ci] = sum_p dz[p][co] x[p + off(tap)][ci]
+// as a GEMM with M = COUT, N = 9*CIN, K = pixels; db[co] = sum_p dz[p][co].
+// Block b walks row segments b, b + G, ...; A (dz, stored [p][co]) and B (the
+// shifted input, stored [p][ci]) fragments come from ldmatrix.trans.  Each
+// block writes its partial sums; k_sum_partials adds them in block order.
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(128) k_conv_dw(const bf16 *__restrict__ x, const bf16 *__restrict__ dz,
+                                                 float *__restrict__ part, int N, int H, int W) {
+  constexpr int PS = CIN + 8, ZS = COUT + 8;
+  constexpr int MT = COUT / 16;
+  constexpr int NTT = 9 * CIN / 8;
+  constexpr int NPW = (NTT + 3) / 4;
+  constexpr int NW = COUT * 9 * CIN + COUT;
+  constexpr int VX = CIN / 8, VZ = COUT / 8;
+  __shared__ __align__(16) bf16 sx[3][TP + 2][PS];
+  __shared__ __align__(16) bf16 sz[TP][ZS];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  const size_t plane = (size_t)H * W;
+  const int segs = (W + TP - 1) / TP;
+  const long long tiles = (long long)N * H * segs;
+  float acc[MT][NPW][4];
+#pragma unroll
+  for (int m = 0; m < MT; ++m)
+#pragma unroll
+    for (int q = 0; q < NPW; ++q) acc[m][q][0] = acc[m][q][1] = acc[m][q][2] = acc[m][q][3] = 0.f;
+  float bacc = 0.f;
+  for (long long tt = blockIdx.x; tt < tiles; tt += gridDim.x) {
+    const int seg = (int)(tt % segs);
+    const long long rr = tt / segs;
+    const int y = (int)(rr % H), img = (int)(rr / H), x0 = seg * TP;
+    __syncthreads();
+    for (int v = tid; v < 3 * (TP + 2) * VX; v += 128) {
+      const int c8 = v % VX, col = (v / VX) % (TP + 2), r = v / (VX * (TP + 2));
+      const int yy = y + r - 1, xx = x0 + col - 1;
+      uint4 val = make_uint4(0, 0, 0, 0);
+      if (yy >= 0 && yy < H && xx >= 0 && xx < W)
+        val = *reinterpret_cast<const uint4 *>(x + ((size_t)img * plane + (size_t)yy * W + xx) * CIN + c8 * 8);
+      *reinterpret_cast<uint4 *>(&sx[r][col][c8 * 8]) = val;
+    }
+    for (int v = tid; v < TP * VZ; v += 128) {
+      const int c8 = v % VZ, p = v / VZ, xx = x0 + p;
+      uint4 val = make_uint4(0, 0, 0, 0);
+      if (xx < W) val = *reinterpret_cast<const uint4 *>(dz + ((size_t)img * plane + (size_t)y * W + xx) * COUT + c8 * 8);
+      *reinterpret_cast<uint4 *>(&sz[p][c8 * 8]) = val;
+    }
+    __syncthreads();
+    if (tid < COUT)
+      for (int p = 0; p < TP; ++p) bacc += __bfloat162float(sz[p][tid]);
+#pragma unroll
+    for (int ks = 0; ks < TP / 16; ++ks) {
+      const int p0 = ks * 16;
+      uint32_t af[MT][4];
+#pragma unroll
+      for (int m = 0; m < MT; ++m) {
+        const int j = lane >> 3, r = lane & 7;
+        ldsm_x4_trans(af[m], &sz[p0 + (j >> 1) * 8 + r][m * 16 + (j & 1) * 8]);
+      }
+#pragma unroll
+      for (int q = 0; q < NPW; ++q) {
+        const int nt = warp + 4 * q;
+        if (nt < NTT) {
+          const int n0 = nt * 8, tap = n0 / CIN, ci0 = n0 % CIN, dy = tap / 3, dx = tap % 3;
+          const int j = (lane >> 3) & 1, r = lane & 7;
+          uint32_t bfr[2];
+          ldsm_x2_trans(bfr, &sx[dy][p0 + j * 8 + r + dx][ci0]);
+#pragma unroll
+          for (int m = 0; m < MT; ++m) mma_bf16(acc[m][q], af[m], bfr);
+        }
+      }
+    }
+  }
+  float *out = part + (size_t)blockIdx.x * NW;
+#pragma unroll
+  for (int m = 0; m < MT; ++m)
+#pragma unroll
+    for (int q = 0; q < NPW; ++q) {
+      const int nt = warp + 4 * q;
+      if (nt < NTT) {
+        const int nn = nt * 8 + 2 * t, ca = m * 16 + g, cb = ca + 8;
+        out[(size_t)ca * 9 * CIN + nn] = acc[m][q][0];
+        out[(size_t)ca * 9 * CIN + nn + 1] = acc[m][q][1];
+        out[(size_t)cb * 9 * CIN + nn] = acc[m][q][2];
+        out[(size_t)cb * 9 * CIN + nn + 1] = acc[m][q][3];
+      }
+    }
+  if (tid < COUT) out[COUT * 9 * CIN + tid] = bacc;
+}
+
+__global__ void k_sum_partials(const float *part, int nparts, int n, float *out) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int b = 0; b < nparts; ++b) s += part[(size_t)b * n + k];
+    out[k] = s;
+  }
+}
+
+// Wt[ci][tap][co] = W[co][8 - tap][ci]: the weights of the input-gradient convolution.
+__global__ void k_flip(const bf16 *w, bf16 *wt, int cin, int cout) {
+  const int n = cin * 9 * cout;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int co = k % cout, tap = (k / cout) % 9, ci = k / (9 * cout);
+    wt[k] = w[((size_t)co * 9 + (8 - tap)) * cin + ci];
+  }
+}
+
+// Adam on FP32 master weights (gradient clipped elementwise); refreshes the
+// BF16 copy the convolutions read.
+__global__ void k_adam(float *wt, float *m, float *v, const float *grad, bf16 *wbf, int n, float lr, float b1, float b2,
+                       float eps, float c1, float c2, float clip, float gscale) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    float gk = grad[k] * gscale;
+    gk = fminf(fmaxf(gk, -clip), clip);
+    m[k] = b1 * m[k] + (1.f - b1) * gk;
+    v[k] = b2 * v[k] + (1.f - b2) * gk * gk;
+    const float mh = m[k] / c1, vh = v[k] / c2;
+    wt[k] -= lr * mh / (sqrtf(vh) + eps);
+    if (wbf) wbf[k] = __float2bfloat16(wt[k]);
+  }
+}
+
+// Network input of crop b at (y, x): u / su, log(rx / rho) / 4, (u - uprev) / sd,
+// then 13 zero channels.  Cells outside the domain give zeros.
+__global__ void k_features(const tl_warm_crop *crops, int B, int H, int W, bf16 *feat) {
+  const long long n = (long long)B * H * W;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(k % W), y = (int)((k / W) % H), b = (int)(k / ((long long)H * W));
+    const tl_warm_crop cr = crops[b];
+    const int gx = cr.ox + x, gy = cr.oy + y;
+    float f0 = 0.f, f1 = 0.f, f2 = 0.f;
+    if (gx >= 0 && gx < cr.nx && gy >= 0 && gy < cr.ny) {
+      const size_t c = (size_t)gy * cr.pitch + gx;
+      const double u = cr.u[c];
+      f0 = (float)(u * cr.inv_su);
+      f1 = 0.25f * (float)log(cr.rx / cr.rho[c]);
+      f2 = (float)((u - cr.uprev[c]) * cr.inv_sd);
+    }
+    __nv_bfloat162 p0 = __floats2bfloat162_rn(f0, f1), p1 = __floats2bfloat162_rn(f2, 0.f);
+    uint4 v0 = make_uint4(*reinterpret_cast<uint32_t *>(&p0), *reinterpret_cast<uint32_t *>(&p1), 0, 0);
+    uint4 *dst = reinterpret_cast<uint4 *>(feat + k * 16);
+    dst[0] = v0;
+    dst[1] = make_uint4(0, 0, 0, 0);
+  }
+}
+
+// Face coefficient between two cells of the crop's domain (0 across the domain
+// boundary: the reflective halo carries no flux).
+__device__ __forceinline__ double face_k(const tl_warm_crop &cr, double r, int ax, int ay, int bx, int by) {
+  if (ax < 0 || ay < 0 || bx >= cr.nx || by >= cr.ny) return 0.0;
+  const double ra = cr.rho[(size_t)ay * cr.pitch + ax], rb = cr.rho[(size_t)by * cr.pitch + bx];
+  return r * (ra + rb) / (2.0 * ra * rb);
+}
+
+// (A v)(gx, gy) = v + sum over faces k (v - v_nbr) for a field v given on crop
+// coordinates through `at(x, y)`.
+template <class F>
+__device__ __forceinline__ double apply_a(const tl_warm_crop &cr, int x, int y, F at) {
+  const int gx = cr.ox + x, gy = cr.oy + y;
+  const double v = at(x, y);
+  double s = v;
+  s += face_k(cr, cr.rx, gx - 1, gy, gx, gy) * (v - at(x - 1, y));
+  s += face_k(cr, cr.rx, gx, gy, gx + 1, gy) * (v - at(x + 1, y));
+  s += face_k(cr, cr.ry, gx, gy - 1, gx, gy) * (v - at(x, y - 1));
+  s += face_k(cr, cr.ry, gx, gy, gx, gy + 1) * (v - at(x, y + 1));
+  return s;
+}
+
+// Loss pass 1: r = d - A((1 + g) d) on the crop's loss region
+// [m, W - m) x [m, H - m) with d = u - uprev, in units of the deck's rms
+// increment (s = inv_sd); partial sums of (s r)^2 and (s d)^2 per block and crop.
+__global__ void __launch_bounds__(256) k_loss_resid(const tl_warm_crop *crops, int H, int W, int margin,
+                                                    const float *g, double *resid, double *sums) {
+  const int b = blockIdx.y;
+  const tl_warm_crop cr = crops[b];
+  const float *gb = g + (size_t)b * H * W;
+  double *rb = resid + (size_t)b * H * W;
+  auto d_at = [&](int x, int y) {
+    const size_t c = (size_t)(cr.oy + y) * cr.pitch + (cr.ox + x);
+    return cr.u[c] - cr.uprev[c];
+  };
+  auto x_at = [&](int x, int y) { return (1.0 + (double)gb[(size_t)y * W + x]) * d_at(x, y); };
+  const int LW = W - 2 * margin, LH = H - 2 * margin;
+  double srr = 0.0, sdd = 0.0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < LW * LH; k += gridDim.x * blockDim.x) {
+    const int x = margin + k % LW, y = margin + k / LW;
+    const double d = d_at(x, y);
+    const double r = d - apply_a(cr, x, y, x_at);
+    rb[(size_t)y * W + x] = r;
+    const double rs = r * cr.inv_sd, ds = d * cr.inv_sd;
+    srr += rs * rs;
+    sdd += ds * ds;
+  }
+  __shared__ double s1[256], s2[256];
+  s1[threadIdx.x] = srr;
+  s2[threadIdx.x] = sdd;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      s1[threadIdx.x] += s1[threadIdx.x + w];
+      s2[threadIdx.x] += s2[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    sums[((size_t)b * gridDim.x + blockIdx.x) * 2] = s1[0];
+    sums[((size_t)b * gridDim.x + blockIdx.x) * 2 + 1] = s2[0];
+  }
+}
+
+// Loss pass 2 (one thread per crop): crop_loss[2b] = mean (s r)^2 over the loss
+// region, crop_loss[2b+1] = mean (s d)^2 (the plain start's value).
+__global__ void k_loss_fold(const double *sums, int B, int nblk, double ncells, double *crop_loss) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  double rr = 0.0, dd = 0.0;
+  for (int k = 0; k < nblk; ++k) {
+    rr += sums[((size_t)b * nblk + k) * 2];
+    dd += sums[((size_t)b * nblk + k) * 2 + 1];
+  }
+  crop_loss[2 * b] = rr / ncells;
+  crop_loss[2 * b + 1] = dd / ncells;
+}
+
+// Loss pass 3: for L = mean over crops of crop_loss[2b],
+// dL/dg = -2 s^2 (A r~) d / (ncells B) one cell beyond the loss region (r~ = r
+// on the loss region, 0 elsewhere), written as channel 0 of the output
+// gradient; every other channel and cell gets 0.
+__global__ void k_loss_grad(const tl_warm_crop *crops, int B, int H, int W, int margin, const double *resid,
+                            double ncells, bf16 *dz) {
+  const long long n = (long long)B * H * W;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(k % W), y = (int)((k / W) % H), b = (int)(k / ((long long)H * W));
+    float gv = 0.f;
+    if (x >= margin - 1 && x < W - margin + 1 && y >= margin - 1 && y < H - margin + 1) {
+      const tl_warm_crop cr = crops[b];
+      const double *rb = resid + (size_t)b * H * W;
+      auto r_at = [&](int xx, int yy) {
+        return (xx >= margin && xx < W - margin && yy >= margin && yy < H - margin) ? rb[(size_t)yy * W + xx] : 0.0;
+      };
+      const double ar = apply_a(cr, x, y, r_at);
+      const size_t c = (size_t)(cr.oy + y) * cr.pitch + (cr.ox + x);
+      const double d = cr.u[c] - cr.uprev[c];
+      gv = (float)(-2.0 * ar * d * cr.inv_sd * cr.inv_sd / (ncells * B));
+    }
+    __nv_bfloat162 p0 = __floats2bfloat162_rn(gv, 0.f);
+    uint4 *dst = reinterpret_cast<uint4 *>(dz + k * 16);
+    dst[0] = make_uint4(*reinterpret_cast<uint32_t *>(&p0), 0, 0, 0);
+    dst[1] = make_uint4(0, 0, 0, 0);
+  }
+}
+
+inline int grid_for(long long n) {
+  long long b = (n + 255) / 256;
+  if (b > 152LL * 16) b = 152LL * 16;
+  return (int)(b < 1 ? 1 : b);
+}
+
+template <int CIN, int COUT>
+void launch_conv(const ConvArgs &a, int mode, cudaStream_t st) {
+  const dim3 grid((a.W + TP - 1) / TP, (a.H + RB - 1) / RB, a.N);
+  if (mode == 0) k_conv3x3<CIN, COUT, 0><<<grid, 128, 0, st>>>(a);
+  else if (mode == 1) k_conv3x3<CIN, COUT, 1><<<grid, 128, 0, st>>>(a);
+  else k_conv3x3<CIN, COUT, 2><<<grid, 128, 0, st>>>(a);
+}
+
+}  // namespace
+
+int tl_conv_forward(const void *x, const void *w, const float *bias, const void *gz, void *z, void *out, float *out32,
+                    int N, int H, int W, int cin, int cout, int mode, cudaStream_t st) {
+  if (!x || !w || (!out && !out32) || N < 1 || H < 1 || W < 1 || mode < 0 || mode > 2) return TL_ERR_ARG;
+  if (mode == 2 && !gz) return TL_ERR_ARG;
+  if (N > 65535 || (H + RB - 1) / RB > 65535) return TL_ERR_ARG;
+  ConvArgs a;
+  a.x = static_cast<const bf16 *>(x);
+  a.w = static_cast<const bf16 *>(w);
+  a.gz = static_cast<const bf16 *>(gz);
+  a.bias = bias;
+  a.z = static_cast<bf16 *>(z);
+  a.out = static_cast<bf16 *>(out);
+  a.out32 = out32;
+  a.N = N;
+  a.H = H;
+  a.W = W;
+  if (cin == 16 && cout == 32) launch_conv<16, 32>(a, mode, st);
+  else if (cin == 32 && cout == 32) launch_conv<32, 32>(a, mode, st);
+  else if (cin == 32 && cout == 16) launch_conv<32, 16>(a, mode, st);
+  else return TL_ERR_ARG;
+  return cudaGetLastError() == cudaSuccess ? TL_OK : TL_ERR_CUDA;
+}
+
+extern "C" int tl_conv3x3_forward(const void *x, const void *w, const float *bias, const void *gz, void *z, void *out,
+                                  float *out32, int N, int H, int W, int cin, int cout, int mode, void *stream) {
+  return tl_conv_forward(x, w, bias, gz, z, out, out32, N, H, W, cin, cout, mode, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int tl_conv3x3_weight_grad(const void *x, const void *dz, float *partials, int nparts, float *dw, int N,
+                                      int H, int W, int cin, int cout, void *stream) {
+  if (!x || !dz || !partials || !dw || nparts < 1 || N < 1 || H < 1 || W < 1) return TL_ERR_ARG;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  auto X = static_cast<const bf16 *>(x);
+  auto Z = static_cast<const bf16 *>(dz);
+  const int nw = cout * 9 * cin + cout;
+  if (cin == 16 && cout == 32) k_conv_dw<16, 32><<<nparts, 128, 0, st>>>(X, Z, partials, N, H, W);
+  else if (cin == 32 && cout == 32) k_conv_dw<32, 32><<<nparts, 128, 0, st>>>(X, Z, partials, N, H, W);
+  else if (cin == 32 && cout == 16) k_conv_dw<32, 16><<<nparts, 128, 0, st>>>(X, Z, partials, N, H, W);
+  else return TL_ERR_ARG;
+  k_sum_partials<<<grid_for(nw), 256, 0, st>>>(partials, nparts, nw, dw);
+  return cudaGetLastError() == cudaSuccess ? TL_OK : TL_ERR_CUDA;
+}
+
+extern "C" int tl_conv3x3_flip(const void *w, void *wt, int cin, int cout, void *stream) {
+  if (!w || !wt || cin < 1 || cout < 1) return TL_ERR_ARG;
+  k_flip<<<grid_for((long long)cin * 9 * cout), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      static_cast<const bf16 *>(w), static_cast<bf16 *>(wt), cin, cout);
+  return cudaGetLastError() == cudaSuccess ? TL_OK : TL_ERR_CUDA;
+}
+
+extern "C" int tl_adam_step(float *w, float *m, float *v, const float *grad, void *wbf16, int n, float lr, float b1,
+                            float b2, float eps, int step, float clip, float gscale, void *stream) {
+  if (!w || !m || !v || !grad || n < 1 || step < 1) return TL_ERR_ARG;
+  const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+  k_adam<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(w, m, v, grad, static_cast<bf16 *>(wbf16), n,
+                                                                      lr, b1, b2, eps, c1, c2, clip, gscale);
+  return cudaGetLastError() == cudaSuccess ? TL_OK : TL_ERR_CUDA;
+}
+
+int tl_warm_features_launch(const tl_warm_crop *crops, int B, int H, int W, void *feat, cudaStream_t st) {
+  k_features<<<grid_for((long long)B * H * W), 256, 0, st>>>(crops, B, H, W, static_cast<bf16 *>(feat));
+  return cudaGetLastError() == cudaSuccess ? TL_OK : TL_ERR_CUDA;
+}
+
+extern "C" int tl_warm_features(const tl_warm_crop *crops, int B, int H, int W, void *feat, void *stream) {
+  if (!crops || !feat || B < 1 || H < 1 || W < 1) return TL_ERR_ARG;
+  return tl_warm_features_launch(crops, B, H, W, feat, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int tl_warm_loss(const tl_warm_crop *crops, int B, int H, int W, int margin, const float *g, double *resid,
+                            double *sums, int nblk, double *crop_loss, void *dz, void *stream) {
+  if (!crops || !g || !resid || !sums || !crop_loss || !dz || B < 1 || B > 65535 || nblk < 1 || margin < 2 ||
+      W <= 2 * margin || H <= 2 * margin)
+    return TL_ERR_ARG;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  k_loss_resid<<<dim3(nblk, B), 256, 0, st>>>(crops, H, W, margin, g, resid, sums);
+  const double ncells = (double)(W - 2 * margin) * (H - 2 * margin);
+  k_loss_fold<<<(B + 127) / 128, 128, 0, st>>>(sums, B, nblk, ncells, crop_loss);
+  k_loss_grad<<<grid_for((long long)B * H * W), 256, 0, st>>>(crops, B, H, W, margin, resid, ncells,
+                                                               static_cast<bf16 *>(dz));
+  return cudaGetLastError() == cudaSuccess ? TL_OK : TL_ERR_CUDA;
+}

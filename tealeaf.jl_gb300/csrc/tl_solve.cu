@@ -342,6 +342,7 @@ int tl_cg_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_resu
   if ((rc = tl_halo_update(ctx, 1, up, 2, 1))) return rc;   // CG.jl:11
   if ((rc = tl_copy_u(ctx))) return rc;                     // CG.jl:12
   ctx->launches += 3;
+  if (prm->warmstart && (rc = tl_warm_try(ctx, rx, ry, res))) return rc;
   ctx->last_solve_ms = 0.0;
   const int which = ref ? TL_GRAPH_CG_REF : (exact ? TL_GRAPH_CG_EXACT : TL_GRAPH_CG_FAST);
   double rel = -1.0;
@@ -383,6 +384,8 @@ int tl_cg_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_resu
 extern "C" int tl_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res) {
   if (!ctx || !prm || !res) return TL_ERR_ARG;
   memset(res, 0, sizeof *res);
+  res->r0_plain = -1.0;
+  res->r0_pred = -1.0;
   if (!ctx->initialised) {
     tl_set_error(ctx, "solve before initialise/set_states");
     return TL_ERR_STATE;

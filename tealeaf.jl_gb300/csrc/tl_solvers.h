@@ -17,7 +17,8 @@ enum {
   TL_NGRAPH
 };
 
-struct tl_ir_state;  // FP32 refinement buffers (tl_ir.cu)
+struct tl_ir_state;    // FP32 refinement buffers (tl_ir.cu)
+struct tl_warm_state;  // warm-start network and its buffers (tl_warm.cu)
 
 struct tl_ctx {
   tl_config cfg{};
@@ -45,6 +46,7 @@ struct tl_ctx {
   cudaGraphExec_t graph[TL_NGRAPH] = {};
   int ppcg_graph_inner = -1;  // inner sweeps recorded in the PPCG graphs
   tl_ir_state *ir = nullptr;
+  tl_warm_state *warm = nullptr;  // learned warm start (tl_warm.cu)
   char msg[512] = {};
 };
 
@@ -82,6 +84,11 @@ int tl_jacobi_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_
 int tl_ir_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res);
 int tl_ir_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch);
 tl::Walk *tl_ir_walk(tl_ctx *ctx, int kernel);  // the FP32 kernels' layouts (kernel 2, 3)
+
+// learned warm start (tl_warm.cu): after init + copyu!, maybe replace the
+// plain start by the network's prediction; always records u^n for the next step.
+int tl_warm_try(tl_ctx *ctx, double rx, double ry, tl_result *res);
+void tl_release_warm(tl_ctx *ctx);
 
 #define CK(x)                                                     \
   do {                                                            \

@@ -91,6 +91,7 @@ class Settings:
     precision: int = _abi.PREC_FP64
     criterion: int = _abi.CRIT_REFERENCE
     exact: bool = False
+    warmstart: bool = False    # CG from the learned prediction when it beats the plain start
 
     def resettoexchange(self):        # settings.jl:80
         for k in self.toexchange:

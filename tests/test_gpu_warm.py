@@ -1,0 +1,170 @@
+"""GPU checks of the warm-start network kernels against the CPU oracle
+(oracle/warmstart_oracle.py), the trainer, and the warm start inside CG.
+
+Per-kernel checks feed the oracle the same BF16 inputs the kernels read, so
+each comparison isolates one kernel: BF16 outputs agree to one BF16 rounding
+(2^-8 relative) plus FP32 accumulation, FP32 outputs to 1e-5, the FP64 loss to
+1e-10.  The end-to-end gradient (oracle forward + backward with BF16 rounding
+at the same points) agrees per layer to 5e-2 in norm: a different FP32
+summation order can flip a BF16 rounding, which then propagates.
+"""
+import numpy as np
+import pytest
+
+import warmstart_oracle as W
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+ULP = 2.0 ** -8
+
+
+def deck_arrays(ny=40, nx=56, seed=0):
+    rng = np.random.default_rng(seed)
+    rho = np.full((ny, nx), 100.0)
+    for _ in range(4):
+        x0, y0 = rng.integers(0, nx - 10), rng.integers(0, ny - 10)
+        rho[y0:y0 + 10, x0:x0 + 14] = 10 ** rng.uniform(-1, 2)
+    yy, xx = np.mgrid[0:ny, 0:nx]
+    base = 1.0 + np.sin(xx / 6.0) * np.cos(yy / 9.0)
+    u = base + 0.2 * (rho < 50) + 0.05 * rng.standard_normal((ny, nx))
+    up = u - 0.03 * base - 0.01 * rng.standard_normal((ny, nx))
+    return u, up, rho
+
+
+def setup(tl, B_crops, H, W_, params, margin=3, rx=5.0):
+    u, up, rho = deck_arrays()
+    dev = {k: torch.tensor(v, dtype=torch.float64, device="cuda") for k, v in (("u", u), ("up", up), ("rho", rho))}
+    ocrops = [W.Crop(u, up, rho, ox, oy, H, W_, rx, rx) for ox, oy in B_crops]
+    ny, nx = u.shape
+    gcrops = [tl._abi.WarmCrop(dev["u"].data_ptr(), dev["up"].data_ptr(), dev["rho"].data_ptr(), nx, nx, ny, c.ox,
+                               c.oy, rx, rx, c.inv_su, c.inv_sd) for c in ocrops]
+    tr = tl.warmstart.Trainer(params, len(ocrops), H, W_, margin=margin, keep_grads=True)
+    tr.set_crops(gcrops)
+    return tr, ocrops, dev
+
+
+def f64(t):
+    return t.detach().float().cpu().numpy().astype(np.float64)
+
+
+def close_bf16(gpu, ref, what):
+    tol = ULP * np.abs(ref) + 1e-5 * max(np.max(np.abs(ref)), 1e-30)
+    bad = np.abs(gpu - ref) > tol
+    assert not bad.any(), f"{what}: {bad.sum()} of {bad.size} beyond one BF16 rounding, max {np.max(np.abs(gpu - ref))}"
+
+
+@pytest.fixture(scope="module")
+def run(tl, built_lib):
+    rng = np.random.default_rng(7)
+    p = W.init_params(11, out_scale=0.05)
+    p = (p + 0.02 * rng.standard_normal(p.size).astype(np.float32) * (p != 0)).astype(np.float32)
+    tr, ocrops, dev = setup(tl, [(3, 2), (12, 14)], 24, 40, p)
+    tr.forward()
+    tr.loss()
+    tr.backward()
+    torch.cuda.synchronize()
+    return tr, ocrops, p, dev
+
+
+def test_features(run):
+    tr, ocrops, p, _ = run
+    ref = W.features(ocrops, rounded=True)
+    close_bf16(f64(tr.feat), ref, "features")
+
+
+def test_forward_layers(run):
+    tr, ocrops, p, _ = run
+    layers = W.unpack(p.astype(np.float64))
+    x = f64(tr.feat)
+    for l in range(5):
+        w, b = layers[l]
+        z = W.conv(x, W.bf16(w)) + b
+        close_bf16(f64(tr.z[l]), W.bf16(z), f"z{l}")
+        close_bf16(f64(tr.a[l]), W.bf16(W.gelu(z)), f"a{l}")
+        x = f64(tr.a[l])
+    w, b = layers[5]
+    g = (W.conv(x, W.bf16(w)) + b)[..., 0]
+    gg = tr.g.cpu().numpy().astype(np.float64)
+    assert np.max(np.abs(gg - g)) <= 1e-5 * np.max(np.abs(g))
+
+
+def test_loss_and_output_gradient(run):
+    tr, ocrops, p, _ = run
+    g = tr.g.cpu().numpy().astype(np.float64)
+    L, terms, dg = W.loss(ocrops, g, tr.margin)
+    cl = tr.crop_loss.cpu().numpy()
+    for b, (a, plain) in enumerate(terms):
+        assert cl[b, 0] == pytest.approx(a, rel=1e-10)
+        assert cl[b, 1] == pytest.approx(plain, rel=1e-10)
+    dz = f64(tr.dz_out)
+    assert np.all(dz[..., 1:] == 0)
+    close_bf16(dz[..., 0], W.bf16(np.float32(dg)), "dL/dg")
+
+
+def test_weight_and_input_gradients(run):
+    tr, ocrops, p, _ = run
+    layers = W.unpack(p.astype(np.float64))
+    grad = tr.grad.cpu().numpy().astype(np.float64)
+    offs = [o for o in __import__("itertools").accumulate([0] + [co * 9 * ci + co for ci, co in W.LAYERS])]
+    for l in range(6):
+        ci, co = W.LAYERS[l]
+        x = f64(tr.feat) if l == 0 else f64(tr.a[l - 1])
+        dz = f64(tr.dz_out) if l == 5 else f64(tr.dz[l])
+        dw, db = W.conv_weight_grad(x, dz)
+        ref = np.concatenate([dw.ravel(), db])
+        got = grad[offs[l]:offs[l + 1]]
+        assert np.linalg.norm(got - ref) <= 1e-5 * np.linalg.norm(ref) + 1e-30, f"weight grad {l}"
+        if l > 0:
+            dx = W.conv_input_grad(dz, W.bf16(layers[l][0]))
+            ref_dz = W.bf16(dx * W.gelu_grad(f64(tr.z[l - 1])))
+            close_bf16(f64(tr.dz[l - 1]), ref_dz, f"input grad {l}")
+
+
+def test_end_to_end_gradient(run):
+    tr, ocrops, p, _ = run
+    feat = W.features(ocrops, rounded=True)
+    g, saved = W.forward(p.astype(np.float64), feat, rounded=True)
+    _, _, dg = W.loss(ocrops, g, tr.margin)
+    ref = W.backward(p.astype(np.float64), saved, dg, rounded=True)
+    got = tr.grad.cpu().numpy().astype(np.float64)
+    k = 0
+    for l, (ci, co) in enumerate(W.LAYERS):
+        n = co * 9 * ci + co
+        r, gg = ref[k:k + n], got[k:k + n]
+        assert np.linalg.norm(gg - r) <= 5e-2 * np.linalg.norm(r), f"layer {l}"
+        k += n
+
+
+def test_training_reduces_loss_on_a_fixed_batch(tl, built_lib):
+    p = W.init_params(5)
+    tr, ocrops, dev = setup(tl, [(3, 2), (12, 14), (0, 0), (16, 16)], 24, 40, p)
+    first = None
+    for it in range(120):
+        tr.forward()
+        tr.loss()
+        if it == 0:
+            first = tr.crop_loss[:, 0].mean().item()
+        tr.backward()
+        tr.adam(2e-3)
+    tr.forward()
+    tr.loss()
+    last = tr.crop_loss[:, 0].mean().item()
+    assert np.isfinite(last) and last < 0.5 * first, (first, last)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_warm_start_judge_and_accuracy(tl, built_lib, precision):
+    """CG from the prediction: every solve meets eps on the true residual, the
+    prediction is used only when its initial residual is below the plain
+    start's, and the final field matches the plain-start run."""
+    params = W.init_params(0)
+    if (tl.warmstart.NET_FILE).exists():
+        params = tl.warmstart.load_params()
+    ev = tl.warmstart.evaluate(tl, params, 128, 424242, 10, precision)
+    w = ev["warm"]
+    assert w["used"][0] == 0                       # no previous step yet
+    for used, a, b in zip(w["used"][1:], w["r0_pred"][1:], w["r0_plain"][1:]):
+        assert used in (1, 2)
+        assert (used == 1) == (a < b)
+    assert ev["final_rel_diff"] < 1e-7
