@@ -29,7 +29,19 @@ from pathlib import Path
 
 import numpy as np
 
-from . import _abi
+if __name__ == "__main__" and not __package__:
+    # run as a script: load the package (its directory name is not an
+    # importable identifier) and run this module's main from inside it
+    import importlib.util
+    _dir = Path(__file__).resolve().parent
+    _spec = importlib.util.spec_from_file_location("tealeaf_gb300", _dir / "__init__.py",
+                                                   submodule_search_locations=[str(_dir)])
+    _mod = importlib.util.module_from_spec(_spec)
+    sys.modules["tealeaf_gb300"] = _mod
+    _spec.loader.exec_module(_mod)
+    sys.exit(_mod.warmstart.main())
+
+from . import _abi  # noqa: E402
 
 MAGIC = b"TLWS"
 VERSION = 1
@@ -408,14 +420,3 @@ def main(argv=None):
     save_params(a.out, params, meta)
     log(f"saved {a.out}")
     return 0
-
-
-if __name__ == "__main__":
-    import importlib.util
-    _dir = Path(__file__).resolve().parent
-    _spec = importlib.util.spec_from_file_location("tealeaf_gb300", _dir / "__init__.py",
-                                                   submodule_search_locations=[str(_dir)])
-    _mod = importlib.util.module_from_spec(_spec)
-    sys.modules["tealeaf_gb300"] = _mod
-    _spec.loader.exec_module(_mod)
-    sys.exit(_mod.warmstart.main())

@@ -2,8 +2,9 @@
 (oracle/warmstart_oracle.py), the trainer, and the warm start inside CG.
 
 Per-kernel checks feed the oracle the same BF16 inputs the kernels read, so
-each comparison isolates one kernel: BF16 outputs agree to one BF16 rounding
-(2^-8 relative) plus FP32 accumulation, FP32 outputs to 1e-5, the FP64 loss to
+each comparison isolates one kernel: BF16 outputs agree to one BF16 unit in
+the last place (at most 2^-7 relative: a different FP32 summation order or
+tanh can move a value across a rounding boundary) plus FP32 accumulation, FP32 outputs to 1e-5, the FP64 loss to
 1e-10.  The end-to-end gradient (oracle forward + backward with BF16 rounding
 at the same points) agrees per layer to 5e-2 in norm: a different FP32
 summation order can flip a BF16 rounding, which then propagates.
@@ -16,7 +17,7 @@ import warmstart_oracle as W
 pytestmark = pytest.mark.gpu
 
 torch = pytest.importorskip("torch")
-ULP = 2.0 ** -8
+ULP = 2.0 ** -7
 
 
 def deck_arrays(ny=40, nx=56, seed=0):
