@@ -92,9 +92,11 @@ typedef struct {
   int precision;            /* TL_PREC_*                                     */
   int exact;                /* 1: tealeaf mode reproduces the reference's operation order with no FMA
                                contraction (bit-identical to the CPU restatement); 0: fused FMA kernels */
-  int warmstart;            /* CG in tealeaf mode: start from the warm-start network's prediction when
-                               its initial residual is below the plain start's (tl_warm_load) */
+  int warmstart;            /* CG in tealeaf mode: 0 off; TL_WARM_NETWORK: start from the warm-start
+                               network's prediction when it beats the plain start (tl_warm_load);
+                               TL_WARM_EXTRAPOLATE: the same with u^n + (u^n - u^{n-1}), no network */
 } tl_params;
+enum { TL_WARM_OFF = 0, TL_WARM_NETWORK = 1, TL_WARM_EXTRAPOLATE = 2 };
 
 typedef struct {
   int iters;                /* trips of the solver's main loop                  */
@@ -108,7 +110,8 @@ typedef struct {
   double rel_residual;      /* ||u0 - A u|| / ||u0|| after the solve (TL_CRIT_RELATIVE), else -1 */
   int launches;             /* kernels this solve launched (graph-body kernels counted per trip) */
   int warm;                 /* 0: plain start (no warm start asked or no previous step), 1: the
-                               prediction was used, 2: the prediction lost to the plain start */
+                               prediction was used, 2: the prediction lost to the plain start,
+                               3: no prediction (paused after a prediction that cost iterations) */
   double r0_plain;          /* ||u0 - A u^n|| / ||u0|| of the plain start (warm start asked), else -1 */
   double r0_pred;           /* the same for the prediction, -1 when none was made */
 } tl_result;
@@ -239,7 +242,9 @@ int tl_field_summary_noalloc(const double *volume, const double *density, const 
  * (u^n - u^{n-1}) / rms(u^n - u^{n-1}) and returns a factor g; the predicted
  * solution is u^n + (1 + g) (u^n - u^{n-1}).  CG starts from it only when its
  * residual ||u^n - A x|| is below the plain start's; it must still meet eps on
- * the true residual.
+ * the true residual.  A solve from the prediction that needs more iterations
+ * than the last solve from the plain start pauses the prediction for 4, 8,
+ * ... 64 steps (a smaller initial residual does not imply fewer iterations).
  *
  * Parameter vector (FP32, TL_WARM_NPARAMS values), layer by layer:
  * W[cout][9][cin] then b[cout], with (cin, cout) = (16, 32), (32, 32) x 4,

@@ -21,6 +21,7 @@ SOLVER_CG, SOLVER_CHEBY, SOLVER_PPCG, SOLVER_JACOBI = 0, 1, 2, 3
 CRIT_REFERENCE, CRIT_RELATIVE = 0, 1
 PREC_FP64, PREC_FP32_IR = 0, 1
 GEOM_RECTANGULAR, GEOM_CIRCULAR, GEOM_POINT = 0, 1, 2
+WARM_OFF, WARM_NETWORK, WARM_EXTRAPOLATE = 0, 1, 2
 
 
 class Config(C.Structure):

@@ -538,7 +538,7 @@ int tl_ir_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_resu
   const int up[2] = {TL_EX_U, TL_EX_P};
   if ((rc = tl_halo_update(ctx, 1, up, 2, 1))) return rc;
   if ((rc = tl_copy_u(ctx))) return rc;
-  if (prm->warmstart && (rc = tl_warm_try(ctx, rx, ry, res))) return rc;
+  if (prm->warmstart && (rc = tl_warm_try(ctx, rx, ry, prm->warmstart, res))) return rc;
   const G32 g32 = g32_of(ctx);
   tl_ir_state *ir = ctx->ir;
   k_ir_convert<<<grid_for((long long)ctx->g.X * ctx->g.Y), 256, 0, ctx->stream>>>(ctx->F, ctx->g, g32, ir->kx, ir->ky,
@@ -601,6 +601,7 @@ int tl_ir_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_resu
   res->converged = rel < p.eps;
   res->refinements = refinements;
   res->launches = (int)ctx->launches;
+  if (prm->warmstart) tl_warm_after(ctx, res);
   return TL_OK;
 }
 

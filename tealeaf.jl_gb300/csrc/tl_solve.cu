@@ -342,7 +342,7 @@ int tl_cg_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_resu
   if ((rc = tl_halo_update(ctx, 1, up, 2, 1))) return rc;   // CG.jl:11
   if ((rc = tl_copy_u(ctx))) return rc;                     // CG.jl:12
   ctx->launches += 3;
-  if (prm->warmstart && (rc = tl_warm_try(ctx, rx, ry, res))) return rc;
+  if (prm->warmstart && (rc = tl_warm_try(ctx, rx, ry, prm->warmstart, res))) return rc;
   ctx->last_solve_ms = 0.0;
   const int which = ref ? TL_GRAPH_CG_REF : (exact ? TL_GRAPH_CG_EXACT : TL_GRAPH_CG_FAST);
   double rel = -1.0;
@@ -378,6 +378,7 @@ int tl_cg_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_resu
   res->converged = ran && (prm->criterion == TL_CRIT_RELATIVE ? (rel >= 0 && rel < prm->eps) : sc.converged);
   res->rel_residual = rel;
   res->launches = (int)ctx->launches;
+  if (prm->warmstart) tl_warm_after(ctx, res);
   return TL_OK;
 }
 

@@ -28,6 +28,8 @@ struct tl_warm_state {
   double *stats = nullptr;              // block partials of u.u and d.d, then the two totals
   tl_warm_crop *crop = nullptr;         // device copy of the whole-domain crop
   int have_prev = 0;
+  int last_plain_iters = -1;            // iterations of the last solve from the plain start
+  int cooloff = 0, backoff = 4;         // the iteration guard (tl_warm_after)
 };
 
 namespace tl {
@@ -191,13 +193,17 @@ extern "C" int tl_warm_load(tl_ctx *ctx, const float *params, int nparams) {
     off += TL_WARM_COUT[l];
   }
   CK(cudaStreamSynchronize(ctx->stream));
-  ws->have_prev = 0;
-  return TL_OK;
+  return tl_warm_reset(ctx);
 }
 
 extern "C" int tl_warm_reset(tl_ctx *ctx) {
   if (!ctx) return TL_ERR_ARG;
-  if (ctx->warm) ctx->warm->have_prev = 0;
+  if (tl_warm_state *ws = ctx->warm) {
+    ws->have_prev = 0;
+    ws->last_plain_iters = -1;
+    ws->cooloff = 0;
+    ws->backoff = 4;
+  }
   return TL_OK;
 }
 
@@ -221,15 +227,23 @@ static int ensure_warm_buffers(tl_ctx *ctx) {
 }
 
 // Called by the CG solves after tea_leaf_init, the halo and copyu!.
-int tl_warm_try(tl_ctx *ctx, double rx, double ry, tl_result *res) {
-  tl_warm_state *ws = ctx->warm;
-  if (!ws || !ws->wbuf) {
-    tl_set_error(ctx, "warm start asked before tl_warm_load");
-    return TL_ERR_STATE;
+int tl_warm_try(tl_ctx *ctx, double rx, double ry, int warmstart, tl_result *res) {
+  if (warmstart != TL_WARM_NETWORK && warmstart != TL_WARM_EXTRAPOLATE) {
+    tl_set_error(ctx, "unknown warm-start mode %d", warmstart);
+    return TL_ERR_ARG;
   }
   if (ctx->cfg.mode != TL_MODE_TEALEAF) {
     tl_set_error(ctx, "the warm start needs the tealeaf (5-point) semantics");
     return TL_ERR_ARG;
+  }
+  if (!ctx->warm) {
+    ctx->warm = new (std::nothrow) tl_warm_state();
+    if (!ctx->warm) return TL_ERR_NOMEM;
+  }
+  tl_warm_state *ws = ctx->warm;
+  if (warmstart == TL_WARM_NETWORK && !ws->wbuf) {
+    tl_set_error(ctx, "warm start asked before tl_warm_load");
+    return TL_ERR_STATE;
   }
   int rc = ensure_warm_buffers(ctx);
   if (rc) return rc;
@@ -241,7 +255,11 @@ int tl_warm_try(tl_ctx *ctx, double rx, double ry, tl_result *res) {
   res->r0_plain = bb > 0 ? sqrt(rr_plain / bb) : sqrt(rr_plain);
   res->r0_pred = -1.0;
   res->warm = 0;
-  if (ws->have_prev) {
+  const int extrapolate = warmstart == TL_WARM_EXTRAPOLATE;
+  if (ws->have_prev && ws->cooloff > 0) {
+    --ws->cooloff;
+    res->warm = 3;
+  } else if (ws->have_prev) {
     k_warm_stats<<<STAT_BLOCKS, 256, 0, st>>>(F, g, ws->uprev, ws->stats);
     k_warm_stats_fold<<<1, 1, 0, st>>>(ws->stats, STAT_BLOCKS);
     CKL();
@@ -263,22 +281,27 @@ int tl_warm_try(tl_ctx *ctx, double rx, double ry, tl_result *res) {
       cr.inv_su = 1.0 / sqrt(tot[0] / cells);
       cr.inv_sd = 1.0 / sqrt(tot[1] / cells);
       CK(cudaMemcpyAsync(ws->crop, &cr, sizeof cr, cudaMemcpyHostToDevice, st));
-      if ((rc = tl_warm_features_launch(ws->crop, 1, g.ny, g.nx, ws->feat, st))) {
-        tl_set_error(ctx, "warm-start feature kernel failed to launch");
-        return rc;
-      }
-      const __nv_bfloat16 *in = ws->feat;
-      __nv_bfloat16 *bufs[2] = {ws->a0, ws->a1};
-      for (int l = 0; l < TL_WARM_LAYERS; ++l) {
-        const int last = l == TL_WARM_LAYERS - 1;
-        __nv_bfloat16 *out = last ? nullptr : bufs[l & 1];
-        rc = tl_conv_forward(in, ws->w[l], ws->b[l], nullptr, nullptr, out, last ? ws->g : nullptr, 1, g.ny, g.nx,
-                             TL_WARM_CIN[l], TL_WARM_COUT[l], last ? 0 : 1, st);
-        if (rc) {
-          tl_set_error(ctx, "warm-start convolution %d failed to launch", l);
+      if (extrapolate) {
+        CK(cudaMemsetAsync(ws->g, 0, sizeof(float) * (size_t)g.nx * g.ny, st));   // g = 0: u^n + (u^n - u^{n-1})
+      } else {
+        if ((rc = tl_warm_features_launch(ws->crop, 1, g.ny, g.nx, ws->feat, st))) {
+          tl_set_error(ctx, "warm-start feature kernel failed to launch");
           return rc;
         }
-        in = out;
+        const __nv_bfloat16 *in = ws->feat;
+        __nv_bfloat16 *bufs[2] = {ws->a0, ws->a1};
+        for (int l = 0; l < TL_WARM_LAYERS; ++l) {
+          const int last = l == TL_WARM_LAYERS - 1;
+          __nv_bfloat16 *out = last ? nullptr : bufs[l & 1];
+          rc = tl_conv_forward(in, ws->w[l], ws->b[l], nullptr, nullptr, out, last ? ws->g : nullptr, 1, g.ny,
+                               g.nx, TL_WARM_CIN[l], TL_WARM_COUT[l], last ? 0 : 1, st);
+          if (rc) {
+            tl_set_error(ctx, "warm-start convolution %d failed to launch", l);
+            return rc;
+          }
+          in = out;
+        }
+        ctx->launches += 1 + TL_WARM_LAYERS;
       }
       k_warm_candidate<<<grid_cells(g), 256, 0, st>>>(F, g, ws->uprev, ws->g);
       CKL();
@@ -290,7 +313,7 @@ int tl_warm_try(tl_ctx *ctx, double rx, double ry, tl_result *res) {
       op.g = g;
       launch_walk<1>(st, op, ctx->walk_exact, g.ny);
       CKL();
-      ctx->launches += 1 + TL_WARM_LAYERS + 3;
+      ctx->launches += 3;
       if ((rc = tl_read_scalars(ctx))) return rc;
       const double rr_pred = ctx->host_sc->red[0];
       res->r0_pred = bb > 0 ? sqrt(rr_pred / bb) : sqrt(rr_pred);
@@ -312,4 +335,26 @@ int tl_warm_try(tl_ctx *ctx, double rx, double ry, tl_result *res) {
   ctx->launches += 1;
   ws->have_prev = 1;
   return TL_OK;
+}
+
+// After the solve: the second judgement.  A solve that started from the
+// prediction and needed more iterations than the last plain-start solve
+// pauses the prediction for `backoff` steps (doubling up to 64 on each
+// repeat, back to 4 after a prediction that did not cost iterations).  A
+// smaller initial residual does not imply fewer CG iterations: error the
+// prediction adds across the whole spectrum costs more than the smooth error
+// of the plain start.
+void tl_warm_after(tl_ctx *ctx, const tl_result *res) {
+  tl_warm_state *ws = ctx->warm;
+  if (!ws) return;
+  if (res->warm == 1) {
+    if (ws->last_plain_iters >= 0 && res->iters > ws->last_plain_iters) {
+      ws->cooloff = ws->backoff;
+      ws->backoff = ws->backoff < 64 ? 2 * ws->backoff : 64;
+    } else {
+      ws->backoff = 4;
+    }
+  } else {
+    ws->last_plain_iters = res->iters;
+  }
 }

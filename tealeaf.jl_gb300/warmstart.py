@@ -299,7 +299,7 @@ class Trainer:
         return self.p.detach().cpu().numpy().copy()
 
 
-def train(trajs, steps: int, B: int = 16, size: int = 128, lr: float = 1e-3, seed: int = 0, params=None,
+def train(trajs, steps: int, B: int = 16, size: int = 128, lr: float = 2e-4, seed: int = 0, params=None,
           log=None, margin: int = 7):
     """Adam on random crops of random consecutive pairs; cosine learning-rate
     decay.  Returns (params, history of (step, mean loss, mean plain value))."""
@@ -310,7 +310,7 @@ def train(trajs, steps: int, B: int = 16, size: int = 128, lr: float = 1e-3, see
     for t, k in pairs:
         scales[t, k] = pair_scales(trajs[t], k)
     pairs = [pk for pk in pairs if scales[pk][1] > 0]
-    tr = Trainer(init_params(seed) if params is None else params, B, size, size, margin)
+    tr = Trainer(init_params(seed, out_scale=0.0) if params is None else params, B, size, size, margin)
     hist, acc = [], []
     t0 = time.time()
     for it in range(steps):
@@ -338,15 +338,21 @@ def train(trajs, steps: int, B: int = 16, size: int = 128, lr: float = 1e-3, see
 # A/B evaluation through the solver
 # ---------------------------------------------------------------------------
 
-def evaluate(tl, params, n: int, seed: int, steps: int, precision: int, log=None):
-    """The same deck solved from the plain start and with the warm start:
-    iterations per step, device time per step, and the final u of both."""
-    out = {}
-    for warm in (False, True):
+MODES = {"plain": _abi.WARM_OFF, "network": _abi.WARM_NETWORK, "extrapolate": _abi.WARM_EXTRAPOLATE}
+
+
+def evaluate(tl, params, n: int, seed: int, steps: int, precision: int, modes=("plain", "network", "extrapolate"),
+             log=None):
+    """The same deck solved from the plain start, with the network's warm
+    start and with plain extrapolation (the network with g = 0): iterations,
+    device time and warm-start decision per step, and the final u of each
+    relative to the plain-start run."""
+    out, fields = {}, {}
+    for name in modes:
         s = tl.Settings.from_text(deck_text(n, seed, steps), mode=_abi.MODE_TEALEAF, exact=False,
-                                  criterion=_abi.CRIT_RELATIVE, precision=precision, warmstart=warm)
+                                  criterion=_abi.CRIT_RELATIVE, precision=precision, warmstart=MODES[name])
         chunk = tl.initialiseapp(s)
-        if warm:
+        if MODES[name] == _abi.WARM_NETWORK:
             chunk.warm_load(params)
         rx, ry = s.dtinit / s.dx ** 2, s.dtinit / s.dy ** 2
         iters, ms, used, r0p, r0q = [], [], [], [], []
@@ -359,21 +365,23 @@ def evaluate(tl, params, n: int, seed: int, steps: int, precision: int, log=None
             t = C.c_double()
             chunk.check(chunk.lib.tl_timer_stop(chunk.ctx, C.byref(t)))
             if not r.converged:
-                raise RuntimeError(f"step {k + 1} (warm={warm}) did not converge: {r}")
+                raise RuntimeError(f"step {k + 1} ({name}) did not converge: {r}")
             iters.append(r.iters)
             ms.append(t.value)
             used.append(r.warm)
             r0p.append(r.r0_plain)
             r0q.append(r.r0_pred)
         hd = s.halodepth
-        out["warm" if warm else "plain"] = {"iters": iters, "ms": ms, "used": used, "r0_plain": r0p, "r0_pred": r0q,
-                                            "u": chunk.field("u")[hd:-hd, hd:-hd].copy()}
+        out[name] = {"iters": iters, "ms": ms, "used": used, "r0_plain": r0p, "r0_pred": r0q}
+        fields[name] = chunk.field("u")[hd:-hd, hd:-hd].copy()
         chunk.close()
         if log:
-            log(f"n={n} seed={seed} prec={precision} warm={warm}: iters {sum(iters)} time {sum(ms):.1f} ms "
-                f"used {sum(1 for x in used if x == 1)}/{steps}")
-    uw, up = out["warm"].pop("u"), out["plain"].pop("u")
-    out["final_rel_diff"] = float(np.linalg.norm(uw - up) / np.linalg.norm(up))
+            log(f"n={n} seed={seed} prec={precision} {name}: iters {sum(iters)} time {sum(ms):.1f} ms "
+                f"predictions used {sum(1 for x in used if x == 1)}/{steps}")
+    if "plain" in fields:
+        ref = fields["plain"]
+        for name, u in fields.items():
+            out[name]["final_rel_diff"] = float(np.linalg.norm(u - ref) / np.linalg.norm(ref))
     return out
 
 
@@ -391,7 +399,7 @@ def main(argv=None):
     t.add_argument("--iters", type=int, default=4000)
     t.add_argument("--batch", type=int, default=16)
     t.add_argument("--crop", type=int, default=128)
-    t.add_argument("--lr", type=float, default=1e-3)
+    t.add_argument("--lr", type=float, default=2e-4)
     t.add_argument("--eval-n", type=int, default=2048)
     t.add_argument("--eval-steps", type=int, default=40)
     t.add_argument("--eval-seeds", type=int, nargs="*", default=[900001])
@@ -412,8 +420,8 @@ def main(argv=None):
     evals = []
     for sd in a.eval_seeds:
         for prec in (_abi.PREC_FP64, _abi.PREC_FP32_IR):
-            evals.append({"seed": sd, "precision": prec,
-                          **evaluate(tl, params, a.eval_n, sd, a.eval_steps, prec, log=log)})
+            evals.append({"seed": sd, "n": a.eval_n, "precision": prec,
+                          "runs": evaluate(tl, params, a.eval_n, sd, a.eval_steps, prec, log=log)})
     meta = {"decks512": a.decks512, "decks2048": a.decks2048, "steps512": a.steps512, "steps2048": a.steps2048,
             "iters": a.iters, "batch": a.batch, "crop": a.crop, "lr": a.lr, "history": hist, "eval": evals}
     Path(a.out).parent.mkdir(parents=True, exist_ok=True)

@@ -158,14 +158,33 @@ def test_training_reduces_loss_on_a_fixed_batch(tl, built_lib):
 def test_warm_start_judge_and_accuracy(tl, built_lib, precision):
     """CG from the prediction: every solve meets eps on the true residual, the
     prediction is used only when its initial residual is below the plain
-    start's, and the final field matches the plain-start run."""
+    start's, a prediction that cost iterations pauses the next ones, and the
+    final field matches the plain-start run."""
     params = W.init_params(0)
     if (tl.warmstart.NET_FILE).exists():
         params = tl.warmstart.load_params()
-    ev = tl.warmstart.evaluate(tl, params, 128, 424242, 10, precision)
-    w = ev["warm"]
-    assert w["used"][0] == 0                       # no previous step yet
-    for used, a, b in zip(w["used"][1:], w["r0_pred"][1:], w["r0_plain"][1:]):
-        assert used in (1, 2)
-        assert (used == 1) == (a < b)
-    assert ev["final_rel_diff"] < 1e-7
+    ev = tl.warmstart.evaluate(tl, params, 128, 424242, 12, precision)
+    plain = ev["plain"]
+    for name in ("network", "extrapolate"):
+        w = ev[name]
+        assert w["used"][0] == 0                       # no previous step yet
+        # the guard, restated: a prediction that cost iterations against the
+        # last plain-start solve pauses the next `backoff` steps (4, 8, ... 64)
+        last_plain, paused, backoff = w["iters"][0], 0, 4
+        for k in range(1, 12):
+            used, a, b = w["used"][k], w["r0_pred"][k], w["r0_plain"][k]
+            if paused:
+                assert used == 3
+                paused -= 1
+                last_plain = w["iters"][k]
+                continue
+            assert used in (1, 2)
+            assert (used == 1) == (a < b)
+            if used == 1:
+                if w["iters"][k] > last_plain:
+                    paused, backoff = backoff, min(2 * backoff, 64)
+                else:
+                    backoff = 4
+            else:
+                last_plain = w["iters"][k]
+        assert w["final_rel_diff"] < 1e-7
