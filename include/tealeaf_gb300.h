@@ -111,7 +111,8 @@ typedef struct {
   int launches;             /* kernels this solve launched (graph-body kernels counted per trip) */
   int warm;                 /* 0: plain start (no warm start asked or no previous step), 1: the
                                prediction was used, 2: the prediction lost to the plain start,
-                               3: no prediction (paused after a prediction that cost iterations) */
+                               3: no prediction (paused after predictions that cost iterations),
+                               4: no prediction (a control solve from the plain start) */
   double r0_plain;          /* ||u0 - A u^n|| / ||u0|| of the plain start (warm start asked), else -1 */
   double r0_pred;           /* the same for the prediction, -1 when none was made */
 } tl_result;
@@ -242,9 +243,11 @@ int tl_field_summary_noalloc(const double *volume, const double *density, const 
  * (u^n - u^{n-1}) / rms(u^n - u^{n-1}) and returns a factor g; the predicted
  * solution is u^n + (1 + g) (u^n - u^{n-1}).  CG starts from it only when its
  * residual ||u^n - A x|| is below the plain start's; it must still meet eps on
- * the true residual.  A solve from the prediction that needs more iterations
- * than the last solve from the plain start pauses the prediction for 4, 8,
- * ... 64 steps (a smaller initial residual does not imply fewer iterations).
+ * the true residual.  A smaller initial residual does not imply fewer
+ * iterations, so runs of at most `trust` (2, 4, ... 32) solves from the
+ * prediction are bracketed by control solves from the plain start; a run that
+ * needed more iterations than its controls pauses the prediction for 4, 8,
+ * ... 64 steps and sets trust back to 2.
  *
  * Parameter vector (FP32, TL_WARM_NPARAMS values), layer by layer:
  * W[cout][9][cin] then b[cout], with (cin, cout) = (16, 32), (32, 32) x 4,

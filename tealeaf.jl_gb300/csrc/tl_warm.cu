@@ -28,8 +28,12 @@ struct tl_warm_state {
   double *stats = nullptr;              // block partials of u.u and d.d, then the two totals
   tl_warm_crop *crop = nullptr;         // device copy of the whole-domain crop
   int have_prev = 0;
-  int last_plain_iters = -1;            // iterations of the last solve from the plain start
-  int cooloff = 0, backoff = 4;         // the iteration guard (tl_warm_after)
+  // the iteration guard (tl_warm_after): plain-start control solves bracket
+  // runs of at most `trust` solves from the prediction
+  int ctrl_iters = -1;                  // iterations of the last solve from the plain start
+  int run = 0;                          // solves from the prediction since that control
+  long long run_iters = 0;              // their iterations
+  int trust = 2, cooloff = 0, backoff = 4;
 };
 
 namespace tl {
@@ -200,7 +204,10 @@ extern "C" int tl_warm_reset(tl_ctx *ctx) {
   if (!ctx) return TL_ERR_ARG;
   if (tl_warm_state *ws = ctx->warm) {
     ws->have_prev = 0;
-    ws->last_plain_iters = -1;
+    ws->ctrl_iters = -1;
+    ws->run = 0;
+    ws->run_iters = 0;
+    ws->trust = 2;
     ws->cooloff = 0;
     ws->backoff = 4;
   }
@@ -259,6 +266,8 @@ int tl_warm_try(tl_ctx *ctx, double rx, double ry, int warmstart, tl_result *res
   if (ws->have_prev && ws->cooloff > 0) {
     --ws->cooloff;
     res->warm = 3;
+  } else if (ws->have_prev && (ws->ctrl_iters < 0 || ws->run >= ws->trust)) {
+    res->warm = 4;  // control solve from the plain start
   } else if (ws->have_prev) {
     k_warm_stats<<<STAT_BLOCKS, 256, 0, st>>>(F, g, ws->uprev, ws->stats);
     k_warm_stats_fold<<<1, 1, 0, st>>>(ws->stats, STAT_BLOCKS);
@@ -337,24 +346,34 @@ int tl_warm_try(tl_ctx *ctx, double rx, double ry, int warmstart, tl_result *res
   return TL_OK;
 }
 
-// After the solve: the second judgement.  A solve that started from the
-// prediction and needed more iterations than the last plain-start solve
-// pauses the prediction for `backoff` steps (doubling up to 64 on each
-// repeat, back to 4 after a prediction that did not cost iterations).  A
-// smaller initial residual does not imply fewer CG iterations: error the
-// prediction adds across the whole spectrum costs more than the smooth error
-// of the plain start.
+// After the solve: the second judgement.  A smaller initial residual does
+// not imply fewer CG iterations (error the prediction adds across the whole
+// spectrum costs more than the smooth error of the plain start), so runs of at
+// most `trust` solves from the prediction are bracketed by control solves
+// from the plain start.  When a run's mean iteration count exceeds the mean of
+// its two controls, the prediction pauses for `backoff` steps (4, 8, ... 64)
+// and trust drops to 2; otherwise trust doubles (up to 32) and the backoff
+// returns to 4.
 void tl_warm_after(tl_ctx *ctx, const tl_result *res) {
   tl_warm_state *ws = ctx->warm;
   if (!ws) return;
   if (res->warm == 1) {
-    if (ws->last_plain_iters >= 0 && res->iters > ws->last_plain_iters) {
+    ++ws->run;
+    ws->run_iters += res->iters;
+    return;
+  }
+  if (ws->run > 0 && ws->ctrl_iters >= 0) {
+    const double pred = (double)ws->run_iters / ws->run, plain = 0.5 * (ws->ctrl_iters + res->iters);
+    if (pred > plain) {
       ws->cooloff = ws->backoff;
       ws->backoff = ws->backoff < 64 ? 2 * ws->backoff : 64;
+      ws->trust = 2;
     } else {
+      ws->trust = ws->trust < 32 ? 2 * ws->trust : 32;
       ws->backoff = 4;
     }
-  } else {
-    ws->last_plain_iters = res->iters;
   }
+  ws->run = 0;
+  ws->run_iters = 0;
+  ws->ctrl_iters = res->iters;
 }

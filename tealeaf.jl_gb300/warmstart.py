@@ -299,39 +299,72 @@ class Trainer:
         return self.p.detach().cpu().numpy().copy()
 
 
-def train(trajs, steps: int, B: int = 16, size: int = 128, lr: float = 2e-4, seed: int = 0, params=None,
-          log=None, margin: int = 7):
-    """Adam on random crops of random consecutive pairs; cosine learning-rate
-    decay.  Returns (params, history of (step, mean loss, mean plain value))."""
+def _random_crops(rng, trajs, pairs, scales, B, size):
+    crops = []
+    for _ in range(B):
+        t, k = pairs[rng.integers(len(pairs))]
+        ny, nx = trajs[t].u.shape[1:]
+        oy, ox = int(rng.integers(0, ny - size + 1)), int(rng.integers(0, nx - size + 1))
+        crops.append(crop_struct(trajs[t], k, ox, oy, scales[t, k]))
+    return crops
+
+
+def _pairs(trajs):
+    pairs = [(t, k) for t in range(len(trajs)) for k in range(1, trajs[t].u.shape[0])]
+    scales = {pk: pair_scales(trajs[pk[0]], pk[1]) for pk in pairs}
+    return [pk for pk in pairs if scales[pk][1] > 0], scales
+
+
+def validation_loss(tr: Trainer, batches) -> float:
+    """Mean loss of the current parameters over fixed batches of crops."""
+    tot = 0.0
+    for crops in batches:
+        tr.set_crops(crops)
+        tr.forward()
+        tr.loss()
+        tot += float(tr.crop_loss[:, 0].mean())
+    return tot / len(batches)
+
+
+def train(trajs, steps: int, B: int = 16, size: int = 128, lr: float = 1e-4, seed: int = 0, params=None,
+          log=None, margin: int = 7, val_trajs=None, val_batches: int = 8, val_every: int = 250):
+    """Adam on random crops of random consecutive pairs, cosine learning-rate
+    decay.  With `val_trajs`, the loss on fixed held-out crops is measured at
+    the start and every `val_every` steps and the best parameters are kept
+    (the start, g = 0, is linear extrapolation).  Returns (params, history of
+    (step, training loss, plain value, validation loss))."""
     import torch
     rng = np.random.default_rng(seed)
-    pairs = [(t, k) for t in range(len(trajs)) for k in range(1, trajs[t].u.shape[0])]
-    scales = {}
-    for t, k in pairs:
-        scales[t, k] = pair_scales(trajs[t], k)
-    pairs = [pk for pk in pairs if scales[pk][1] > 0]
+    pairs, scales = _pairs(trajs)
     tr = Trainer(init_params(seed, out_scale=0.0) if params is None else params, B, size, size, margin)
+    val = None
+    if val_trajs:
+        vpairs, vscales = _pairs(val_trajs)
+        vrng = np.random.default_rng(seed + 1)
+        val = [_random_crops(vrng, val_trajs, vpairs, vscales, B, size) for _ in range(val_batches)]
+    best = (validation_loss(tr, val) if val else float("inf"), tr.params(), 0)
     hist, acc = [], []
     t0 = time.time()
     for it in range(steps):
-        crops = []
-        for _ in range(B):
-            t, k = pairs[rng.integers(len(pairs))]
-            ny, nx = trajs[t].u.shape[1:]
-            oy, ox = int(rng.integers(0, ny - size + 1)), int(rng.integers(0, nx - size + 1))
-            crops.append(crop_struct(trajs[t], k, ox, oy, scales[t, k]))
         cur_lr = lr * 0.5 * (1 + np.cos(np.pi * it / steps))
-        tr.step(crops, cur_lr)
+        tr.step(_random_crops(rng, trajs, pairs, scales, B, size), cur_lr)
         if it % 50 == 0 or it == steps - 1:
             acc.append(tr.crop_loss.detach().clone())
-        if (it % 500 == 0 or it == steps - 1) and acc:
-            cl = torch.cat([a for a in acc]).cpu().numpy()
+        last = it == steps - 1
+        if val and ((it + 1) % val_every == 0 or last):
+            v = validation_loss(tr, val)
+            if v < best[0]:
+                best = (v, tr.params(), it + 1)
+        if ((it + 1) % 1000 == 0 or last) and acc:
+            cl = torch.cat(acc).cpu().numpy()
             acc = []
-            hist.append((it, float(cl[:, 0].mean()), float(cl[:, 1].mean())))
+            hist.append((it + 1, float(cl[:, 0].mean()), float(cl[:, 1].mean()), best[0]))
             if log:
-                log(f"step {it}: loss {hist[-1][1]:.4e} plain {hist[-1][2]:.4e} "
-                    f"ratio {hist[-1][1] / max(hist[-1][2], 1e-300):.3e} ({time.time() - t0:.1f} s)")
-    return tr.params(), hist
+                log(f"step {it + 1}: loss {hist[-1][1]:.4e} plain {hist[-1][2]:.4e} best validation "
+                    f"{best[0]:.4e} at step {best[2]} ({time.time() - t0:.1f} s)")
+    if val:
+        return best[1], hist, {"val_loss": best[0], "val_step": best[2]}
+    return tr.params(), hist, {}
 
 
 # ---------------------------------------------------------------------------
@@ -399,7 +432,7 @@ def main(argv=None):
     t.add_argument("--iters", type=int, default=4000)
     t.add_argument("--batch", type=int, default=16)
     t.add_argument("--crop", type=int, default=128)
-    t.add_argument("--lr", type=float, default=2e-4)
+    t.add_argument("--lr", type=float, default=1e-4)
     t.add_argument("--eval-n", type=int, default=2048)
     t.add_argument("--eval-steps", type=int, default=40)
     t.add_argument("--eval-seeds", type=int, nargs="*", default=[900001])
@@ -407,15 +440,18 @@ def main(argv=None):
     log = lambda m: print(m, flush=True)   # noqa: E731
     t0 = time.time()
     trajs = generate(tl, 512, range(1000, 1000 + a.decks512), a.steps512, log=None)
+    val = generate(tl, 512, range(5000, 5004), a.steps512, log=None)
     log(f"generated {a.decks512} trajectories at 512^2 ({time.time() - t0:.1f} s)")
     t1 = time.time()
     trajs += generate(tl, 2048, range(2000, 2000 + a.decks2048), a.steps2048, log=None)
+    val += generate(tl, 2048, range(6000, 6002), a.steps2048, log=None)
     log(f"generated {a.decks2048} trajectories at 2048^2 ({time.time() - t1:.1f} s)")
     t2 = time.time()
-    params, hist = train(trajs, a.iters, a.batch, a.crop, a.lr, log=log)
+    params, hist, sel = train(trajs, a.iters, a.batch, a.crop, a.lr, log=log, val_trajs=val)
+    log(f"selected parameters: {sel}")
     torch.cuda.synchronize()
     log(f"trained {a.iters} steps ({time.time() - t2:.1f} s)")
-    del trajs
+    del trajs, val
     torch.cuda.empty_cache()
     evals = []
     for sd in a.eval_seeds:
@@ -423,7 +459,8 @@ def main(argv=None):
             evals.append({"seed": sd, "n": a.eval_n, "precision": prec,
                           "runs": evaluate(tl, params, a.eval_n, sd, a.eval_steps, prec, log=log)})
     meta = {"decks512": a.decks512, "decks2048": a.decks2048, "steps512": a.steps512, "steps2048": a.steps2048,
-            "iters": a.iters, "batch": a.batch, "crop": a.crop, "lr": a.lr, "history": hist, "eval": evals}
+            "iters": a.iters, "batch": a.batch, "crop": a.crop, "lr": a.lr, "history": hist, "selection": sel,
+            "eval": evals}
     Path(a.out).parent.mkdir(parents=True, exist_ok=True)
     save_params(a.out, params, meta)
     log(f"saved {a.out}")

@@ -168,23 +168,27 @@ def test_warm_start_judge_and_accuracy(tl, built_lib, precision):
     for name in ("network", "extrapolate"):
         w = ev[name]
         assert w["used"][0] == 0                       # no previous step yet
-        # the guard, restated: a prediction that cost iterations against the
-        # last plain-start solve pauses the next `backoff` steps (4, 8, ... 64)
-        last_plain, paused, backoff = w["iters"][0], 0, 4
+        # the guard, restated: runs of at most `trust` solves from the
+        # prediction between plain-start controls; a run that needed more
+        # iterations than the mean of its two controls pauses the prediction
+        ctrl, run, run_iters, trust, cooloff, backoff = w["iters"][0], 0, 0, 2, 0, 4
         for k in range(1, 12):
-            used, a, b = w["used"][k], w["r0_pred"][k], w["r0_plain"][k]
-            if paused:
+            used, a, b, it = w["used"][k], w["r0_pred"][k], w["r0_plain"][k], w["iters"][k]
+            if cooloff:
                 assert used == 3
-                paused -= 1
-                last_plain = w["iters"][k]
-                continue
-            assert used in (1, 2)
-            assert (used == 1) == (a < b)
-            if used == 1:
-                if w["iters"][k] > last_plain:
-                    paused, backoff = backoff, min(2 * backoff, 64)
-                else:
-                    backoff = 4
+                cooloff -= 1
+            elif run >= trust:
+                assert used == 4
             else:
-                last_plain = w["iters"][k]
+                assert used in (1, 2)
+                assert (used == 1) == (a < b)
+            if used == 1:
+                run, run_iters = run + 1, run_iters + it
+                continue
+            if run:
+                if run_iters / run > 0.5 * (ctrl + it):
+                    cooloff, backoff, trust = backoff, min(2 * backoff, 64), 2
+                else:
+                    trust, backoff = min(2 * trust, 32), 4
+            run, run_iters, ctrl = 0, 0, it
         assert w["final_rel_diff"] < 1e-7
