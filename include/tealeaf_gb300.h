@@ -290,14 +290,16 @@ int tl_adam_step(float *w, float *m, float *v, const float *grad, void *wbf16, i
                  float eps, int step, float clip, float gscale, void *stream);
 /* feat[B][H][W][16] = the network input of B crops. */
 int tl_warm_features(const tl_warm_crop *crops, int B, int H, int W, void *feat, void *stream);
-/* Loss of B crops of H x W: L = mean over crops of mean((inv_sd r)^2), r =
- * d - A((1 + g) d), over the cells at least `margin` (>= 2) from the crop
- * edge; d = u - uprev, A the 5-point operator of the crop's deck.
- * crop_loss[2b] = the crop's term, crop_loss[2b+1] = mean((inv_sd d)^2) (the
- * plain start's value); dz[B][H][W][16] = dL/dg in channel 0, 0 elsewhere.
- * resid: B*H*W doubles, sums: B*nblk*2 doubles of scratch. */
-int tl_warm_loss(const tl_warm_crop *crops, int B, int H, int W, int margin, const float *g, double *resid,
-                 double *sums, int nblk, double *crop_loss, void *dz, void *stream);
+/* Loss of B crops of H x W.  Per crop, term = mean((inv_sd r)^2) with
+ * r = d - A((1 + g) d) over the cells at least `margin` (>= 2) from the crop
+ * edge, d = u - uprev, A the 5-point operator of the crop's deck, and
+ * plain = mean((inv_sd d)^2) (the plain start's value).  objective 0:
+ * L = mean of the terms; 1: L = mean of log(term / plain).
+ * crop_loss[2b] = term, crop_loss[2b+1] = plain; dz[B][H][W][16] = dL/dg in
+ * channel 0, 0 elsewhere.  resid: B*H*W doubles, sums: B*nblk*2 doubles of
+ * scratch. */
+int tl_warm_loss(const tl_warm_crop *crops, int B, int H, int W, int margin, int objective, const float *g,
+                 double *resid, double *sums, int nblk, double *crop_loss, void *dz, void *stream);
 
 #ifdef __cplusplus
 }

@@ -162,8 +162,9 @@ def _apply_a(v, k):
             + kn * (c - v[2:, 1:-1]))
 
 
-def loss(crops, g, margin):
-    """(L, per-crop (loss, plain), dL/dg[B, h, w]) of the residual loss (float64)."""
+def loss(crops, g, margin, objective=0):
+    """(L, per-crop (term, plain), dL/dg[B, h, w]) of the residual loss (float64):
+    objective 0 averages the terms, 1 averages log(term / plain)."""
     B = len(crops)
     terms, dg = [], np.zeros(g.shape)
     for b, c in enumerate(crops):
@@ -177,12 +178,18 @@ def loss(crops, g, margin):
         mask[margin:h - margin, margin:w - margin] = True
         ncell = mask.sum()
         s2 = c.inv_sd ** 2
-        terms.append((np.sum((r[mask] ** 2)) * s2 / ncell, np.sum(d[mask] ** 2) * s2 / ncell))
+        term = np.sum((r[mask] ** 2)) * s2 / ncell
+        terms.append((term, np.sum(d[mask] ** 2) * s2 / ncell))
         rt = np.where(mask, r, 0.0)
         ar = _apply_a(np.pad(rt, 1), k)
         band = np.zeros((h, w), dtype=bool)
         band[margin - 1:h - margin + 1, margin - 1:w - margin + 1] = True
-        dg[b] = np.where(band, -2.0 * ar * d * s2 / (ncell * B), 0.0)
+        scale = -2.0 * s2 / (ncell * B)
+        if objective == 1:
+            scale = scale / term if term > 0 else 0.0
+        dg[b] = np.where(band, ar * d * scale, 0.0)
+    if objective == 1:
+        return float(np.mean([np.log(t / p) for t, p in terms])), terms, dg
     return float(np.mean([t[0] for t in terms])), terms, dg
 
 

@@ -107,8 +107,8 @@ SIGNATURES = {
     "tl_adam_step": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_float,
                       C.c_float, C.c_float, C.c_int, C.c_float, C.c_float, C.c_void_p], C.c_int),
     "tl_warm_features": ([C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p], C.c_int),
-    "tl_warm_loss": ([C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
-                      C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "tl_warm_loss": ([C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                      C.c_int, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
 }
 
 _lib = None

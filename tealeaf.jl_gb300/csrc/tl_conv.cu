@@ -386,12 +386,13 @@ __global__ void k_loss_fold(const double *sums, int B, int nblk, double ncells, 
   crop_loss[2 * b + 1] = dd / ncells;
 }
 
-// Loss pass 3: for L = mean over crops of crop_loss[2b],
-// dL/dg = -2 s^2 (A r~) d / (ncells B) one cell beyond the loss region (r~ = r
-// on the loss region, 0 elsewhere), written as channel 0 of the output
-// gradient; every other channel and cell gets 0.
+// Loss pass 3: for L = mean over crops of crop_loss[2b] (objective 0) or of
+// log(crop_loss[2b] / crop_loss[2b+1]) (objective 1),
+// dL/dg = -2 s^2 (A r~) d / (ncells B) [/ crop_loss[2b]] one cell beyond the
+// loss region (r~ = r on the loss region, 0 elsewhere), written as channel 0
+// of the output gradient; every other channel and cell gets 0.
 __global__ void k_loss_grad(const tl_warm_crop *crops, int B, int H, int W, int margin, const double *resid,
-                            double ncells, bf16 *dz) {
+                            double ncells, const double *crop_loss, int objective, bf16 *dz) {
   const long long n = (long long)B * H * W;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
     const int x = (int)(k % W), y = (int)((k / W) % H), b = (int)(k / ((long long)H * W));
@@ -405,7 +406,9 @@ __global__ void k_loss_grad(const tl_warm_crop *crops, int B, int H, int W, int 
       const double ar = apply_a(cr, x, y, r_at);
       const size_t c = (size_t)(cr.oy + y) * cr.pitch + (cr.ox + x);
       const double d = cr.u[c] - cr.uprev[c];
-      gv = (float)(-2.0 * ar * d * cr.inv_sd * cr.inv_sd / (ncells * B));
+      double scale = -2.0 * cr.inv_sd * cr.inv_sd / (ncells * B);
+      if (objective == 1) scale = crop_loss[2 * b] > 0 ? scale / crop_loss[2 * b] : 0.0;
+      gv = (float)(ar * d * scale);
     }
     __nv_bfloat162 p0 = __floats2bfloat162_rn(gv, 0.f);
     uint4 *dst = reinterpret_cast<uint4 *>(dz + k * 16);
@@ -499,8 +502,8 @@ extern "C" int tl_warm_features(const tl_warm_crop *crops, int B, int H, int W, 
   return tl_warm_features_launch(crops, B, H, W, feat, static_cast<cudaStream_t>(stream));
 }
 
-extern "C" int tl_warm_loss(const tl_warm_crop *crops, int B, int H, int W, int margin, const float *g, double *resid,
-                            double *sums, int nblk, double *crop_loss, void *dz, void *stream) {
+extern "C" int tl_warm_loss(const tl_warm_crop *crops, int B, int H, int W, int margin, int objective, const float *g,
+                            double *resid, double *sums, int nblk, double *crop_loss, void *dz, void *stream) {
   if (!crops || !g || !resid || !sums || !crop_loss || !dz || B < 1 || B > 65535 || nblk < 1 || margin < 2 ||
       W <= 2 * margin || H <= 2 * margin)
     return TL_ERR_ARG;
@@ -508,7 +511,8 @@ extern "C" int tl_warm_loss(const tl_warm_crop *crops, int B, int H, int W, int 
   k_loss_resid<<<dim3(nblk, B), 256, 0, st>>>(crops, H, W, margin, g, resid, sums);
   const double ncells = (double)(W - 2 * margin) * (H - 2 * margin);
   k_loss_fold<<<(B + 127) / 128, 128, 0, st>>>(sums, B, nblk, ncells, crop_loss);
-  k_loss_grad<<<grid_for((long long)B * H * W), 256, 0, st>>>(crops, B, H, W, margin, resid, ncells,
+  k_loss_grad<<<grid_for((long long)B * H * W), 256, 0, st>>>(crops, B, H, W, margin, resid, ncells, crop_loss,
+                                                               objective,
                                                                static_cast<bf16 *>(dz));
   return cudaGetLastError() == cudaSuccess ? TL_OK : TL_ERR_CUDA;
 }

@@ -191,11 +191,11 @@ class Trainer:
     """Forward, loss, backward and Adam for B crops of H x W, all in the library."""
 
     def __init__(self, params: np.ndarray, B: int, H: int, W: int, margin: int = 7, keep_grads: bool = False,
-                 device="cuda"):
+                 objective: int = 1, device="cuda"):
         import torch
         self.torch = torch
         self.lib = _abi.load()
-        self.B, self.H, self.W, self.margin = B, H, W, margin
+        self.B, self.H, self.W, self.margin, self.objective = B, H, W, margin, objective
         dev = torch.device(device)
         n = _abi.WARM_NPARAMS
         self.p = torch.tensor(np.asarray(params, dtype=np.float32), device=dev)
@@ -259,7 +259,8 @@ class Trainer:
             self._chk(rc, f"conv layer {l}")
 
     def loss(self):
-        rc = self.lib.tl_warm_loss(self.crops.data_ptr(), self.B, self.H, self.W, self.margin, self.g.data_ptr(),
+        rc = self.lib.tl_warm_loss(self.crops.data_ptr(), self.B, self.H, self.W, self.margin, self.objective,
+                                   self.g.data_ptr(),
                                    self.resid.data_ptr(), self.sums.data_ptr(), self.nblk, self.crop_loss.data_ptr(),
                                    self.dz_out.data_ptr(), self._st())
         self._chk(rc, "loss")
@@ -315,28 +316,38 @@ def _pairs(trajs):
     return [pk for pk in pairs if scales[pk][1] > 0], scales
 
 
+def batch_objective(tr: Trainer) -> float:
+    """The trainer's objective on its current batch (after forward and loss)."""
+    cl = tr.crop_loss.detach().cpu().numpy()
+    if tr.objective == 1:
+        ok = (cl[:, 0] > 0) & (cl[:, 1] > 0)
+        return float(np.mean(np.log(cl[ok, 0] / cl[ok, 1]))) if ok.any() else 0.0
+    return float(cl[:, 0].mean())
+
+
 def validation_loss(tr: Trainer, batches) -> float:
-    """Mean loss of the current parameters over fixed batches of crops."""
+    """The objective of the current parameters over fixed batches of crops."""
     tot = 0.0
     for crops in batches:
         tr.set_crops(crops)
         tr.forward()
         tr.loss()
-        tot += float(tr.crop_loss[:, 0].mean())
+        tot += batch_objective(tr)
     return tot / len(batches)
 
 
 def train(trajs, steps: int, B: int = 16, size: int = 128, lr: float = 1e-4, seed: int = 0, params=None,
-          log=None, margin: int = 7, val_trajs=None, val_batches: int = 8, val_every: int = 250):
+          log=None, margin: int = 7, val_trajs=None, val_batches: int = 8, val_every: int = 250, objective: int = 1):
     """Adam on random crops of random consecutive pairs, cosine learning-rate
     decay.  With `val_trajs`, the loss on fixed held-out crops is measured at
     the start and every `val_every` steps and the best parameters are kept
     (the start, g = 0, is linear extrapolation).  Returns (params, history of
-    (step, training loss, plain value, validation loss))."""
+    (step, mean term, mean plain value, mean log ratio, best validation), selection)."""
     import torch
     rng = np.random.default_rng(seed)
     pairs, scales = _pairs(trajs)
-    tr = Trainer(init_params(seed, out_scale=0.0) if params is None else params, B, size, size, margin)
+    tr = Trainer(init_params(seed, out_scale=0.0) if params is None else params, B, size, size, margin,
+                 objective=objective)
     val = None
     if val_trajs:
         vpairs, vscales = _pairs(val_trajs)
@@ -358,12 +369,14 @@ def train(trajs, steps: int, B: int = 16, size: int = 128, lr: float = 1e-4, see
         if ((it + 1) % 1000 == 0 or last) and acc:
             cl = torch.cat(acc).cpu().numpy()
             acc = []
-            hist.append((it + 1, float(cl[:, 0].mean()), float(cl[:, 1].mean()), best[0]))
+            ok = (cl[:, 0] > 0) & (cl[:, 1] > 0)
+            lr_mean = float(np.mean(np.log(cl[ok, 0] / cl[ok, 1]))) if ok.any() else 0.0
+            hist.append((it + 1, float(cl[:, 0].mean()), float(cl[:, 1].mean()), lr_mean, best[0]))
             if log:
-                log(f"step {it + 1}: loss {hist[-1][1]:.4e} plain {hist[-1][2]:.4e} best validation "
-                    f"{best[0]:.4e} at step {best[2]} ({time.time() - t0:.1f} s)")
+                log(f"step {it + 1}: term {hist[-1][1]:.3e} plain {hist[-1][2]:.3e} mean log ratio {lr_mean:.3f} "
+                    f"best validation {best[0]:.4f} at step {best[2]} ({time.time() - t0:.1f} s)")
     if val:
-        return best[1], hist, {"val_loss": best[0], "val_step": best[2]}
+        return best[1], hist, {"val_objective": best[0], "val_step": best[2], "objective": objective}
     return tr.params(), hist, {}
 
 

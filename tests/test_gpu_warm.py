@@ -33,14 +33,14 @@ def deck_arrays(ny=40, nx=56, seed=0):
     return u, up, rho
 
 
-def setup(tl, B_crops, H, W_, params, margin=3, rx=5.0):
+def setup(tl, B_crops, H, W_, params, margin=3, rx=5.0, objective=0):
     u, up, rho = deck_arrays()
     dev = {k: torch.tensor(v, dtype=torch.float64, device="cuda") for k, v in (("u", u), ("up", up), ("rho", rho))}
     ocrops = [W.Crop(u, up, rho, ox, oy, H, W_, rx, rx) for ox, oy in B_crops]
     ny, nx = u.shape
     gcrops = [tl._abi.WarmCrop(dev["u"].data_ptr(), dev["up"].data_ptr(), dev["rho"].data_ptr(), nx, nx, ny, c.ox,
                                c.oy, rx, rx, c.inv_su, c.inv_sd) for c in ocrops]
-    tr = tl.warmstart.Trainer(params, len(ocrops), H, W_, margin=margin, keep_grads=True)
+    tr = tl.warmstart.Trainer(params, len(ocrops), H, W_, margin=margin, keep_grads=True, objective=objective)
     tr.set_crops(gcrops)
     return tr, ocrops, dev
 
@@ -120,6 +120,19 @@ def test_weight_and_input_gradients(run):
             dx = W.conv_input_grad(dz, W.bf16(layers[l][0]))
             ref_dz = W.bf16(dx * W.gelu_grad(f64(tr.z[l - 1])))
             close_bf16(f64(tr.dz[l - 1]), ref_dz, f"input grad {l}")
+
+
+def test_log_ratio_objective_gradient(tl, built_lib):
+    """Objective 1 (mean log(term / plain)): the output gradient against the oracle."""
+    p = W.init_params(3, out_scale=0.05)
+    tr, ocrops, dev = setup(tl, [(3, 2), (12, 14)], 24, 40, p, objective=1)
+    tr.forward()
+    tr.loss()
+    torch.cuda.synchronize()
+    g = tr.g.cpu().numpy().astype(np.float64)
+    L, terms, dg = W.loss(ocrops, g, tr.margin, objective=1)
+    assert tl.warmstart.batch_objective(tr) == pytest.approx(L, rel=1e-9)
+    close_bf16(f64(tr.dz_out)[..., 0], W.bf16(np.float32(dg)), "dlog/dg")
 
 
 def test_end_to_end_gradient(run):

@@ -109,3 +109,15 @@ def test_committed_network_file(tl):
         pytest.skip("no trained network committed")
     p = tl.warmstart.load_params(path)
     assert p.dtype == np.float32 and p.size == W.NPARAMS and np.all(np.isfinite(p))
+
+
+def test_log_ratio_gradient_matches_finite_differences():
+    u, up, rho = small_deck(seed=6)
+    crops = crops_of(u, up, rho, rx=7.0)
+    g = 0.1 * np.random.default_rng(3).standard_normal((2, 16, 16))
+    _, _, dg = W.loss(crops, g, 3, objective=1)
+    for b, y, x in ((0, 8, 8), (1, 4, 9)):
+        e = np.zeros_like(g)
+        e[b, y, x] = 1e-6
+        fd = (W.loss(crops, g + e, 3, objective=1)[0] - W.loss(crops, g - e, 3, objective=1)[0]) / 2e-6
+        assert abs(fd - dg[b, y, x]) <= 1e-6 * max(abs(fd), 1e-8), (b, y, x, fd, dg[b, y, x])
