@@ -139,10 +139,16 @@ class ClockSampler:
 # the GPU arm
 # ---------------------------------------------------------------------------
 
-def gpu_setup(tl, n, precision, maxiters=40000):
+# bench variants: (precision, warm start); the first one run is the headline
+VARIANTS = {"learned_fp32_ir": (1, 1), "fp32_ir": (1, 0), "extrap_fp32_ir": (1, 2), "fp64": (0, 0)}
+
+
+def gpu_setup(tl, n, precision, maxiters=40000, warm=0):
     s = tl.Settings.from_text(make_deck(n, maxiters=maxiters), mode=1, exact=False, criterion=1,
-                              precision=precision)
+                              precision=precision, warmstart=warm)
     chunk = tl.initialiseapp(s)
+    if warm == tl._abi.WARM_NETWORK:
+        chunk.warm_load(tl.warmstart.load_params())
     return s, chunk
 
 
@@ -155,10 +161,10 @@ def timestep(tl, chunk, s):
     return res
 
 
-def run_variant(tl, n, precision, steps, warmup):
+def run_variant(tl, n, precision, steps, warmup, warm=0):
     """W untimed + K timed timesteps; each timed step bracketed by device events
     on the library's stream."""
-    s, chunk = gpu_setup(tl, n, precision)
+    s, chunk = gpu_setup(tl, n, precision, warm=warm)
     lib = chunk.lib
     for _ in range(warmup):
         r = timestep(tl, chunk, s)
@@ -178,12 +184,12 @@ def run_variant(tl, n, precision, steps, warmup):
     return s, chunk, times, results
 
 
-def run_e2e(tl, n, precision, steps, warmup):
+def run_e2e(tl, n, precision, steps, warmup, warm=0):
     """The same timesteps through the C ABI with host buffers: each step uploads
     energy and density from pinned memory, solves, runs solvefinished and
     downloads energy; the W warm-up steps go through the same path untimed."""
     import torch
-    s, chunk = gpu_setup(tl, n, precision)
+    s, chunk = gpu_setup(tl, n, precision, warm=warm)
     lib = chunk.lib
     X, Y = chunk.size()
     pinned = {nm: torch.empty((Y, X), dtype=torch.float64, pin_memory=True) for nm in ("energy", "density")}
@@ -225,7 +231,7 @@ def kernel_roofline(tl, chunk, variant):
     lib = chunk.lib
     cells = chunk.settings.xcells * chunk.settings.ycells
     out = {}
-    for k, name, b in KERNELS[variant]:
+    for k, name, b in KERNELS["fp64" if VARIANTS[variant][0] == 0 else "fp32_ir"]:
         ms = C.c_double()
         chunk.check(lib.tl_bench_kernel(chunk.ctx, k, 20, C.byref(ms)))
         out[name] = {"ms": ms.value, "bytes_per_cell": b, "gbs": b * cells / (ms.value * 1e-3) / 1e9}
@@ -310,14 +316,14 @@ def gpu_arm(args):
     n = args.size
     variants = {}
     headline = None
-    prec = {"fp64": 0, "fp32_ir": 1}
-    order = ["fp32_ir", "fp64"] if args.variant == "all" else [args.variant]
+    order = list(VARIANTS) if args.variant == "all" else [args.variant]
     with ClockSampler(local) as clk:
         for name in order:
             try:
                 if dist:
                     dist.barrier()
-                s, chunk, times, results = run_variant(tl, n, prec[name], args.steps, args.warmup)
+                prec, warm = VARIANTS[name]
+                s, chunk, times, results = run_variant(tl, n, prec, args.steps, args.warmup, warm=warm)
             except tl.TeaLeafError as e:
                 variants[name] = {"error": str(e)}
                 continue
@@ -335,7 +341,9 @@ def gpu_arm(args):
                               "loop_ms": loop_ms, "launches": [r.launches for r in results],
                               "ms_per_iteration": statistics.mean(loop_ms) / statistics.mean(iters),
                               "algorithmic_gbs_per_iteration": (BYTES_PER_CELL_ITER if name == "fp64" else 48) *
-                              n * n * statistics.mean(iters) / (statistics.mean(loop_ms) * 1e-3) / 1e9}
+                              n * n * statistics.mean(iters) / (statistics.mean(loop_ms) * 1e-3) / 1e9,
+                              "warm": [r.warm for r in results], "r0_plain": [r.r0_plain for r in results],
+                              "r0_pred": [r.r0_pred for r in results]}
             if headline is None:
                 headline = (name, chunk, results)
             else:
@@ -347,11 +355,12 @@ def gpu_arm(args):
     hname, hchunk, hres = headline
     roof = kernel_roofline(tl, hchunk, hname)
     hchunk.close()
-    e2e_ms, h2d, d2h = run_e2e(tl, n, prec[hname], args.steps, args.warmup)
+    e2e_ms, h2d, d2h = run_e2e(tl, n, VARIANTS[hname][0], args.steps, args.warmup, warm=VARIANTS[hname][1])
     value = variants[hname]["ms_per_step"]
     line = {"metric": METRIC, "value": value, "unit": "ms", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if hname == "fp64" else "f32+f64",
+            "vs_baseline": None,
+            "dtype": {"fp64": "f64", "learned_fp32_ir": "f32+f64 (bf16 network)"}.get(hname, "f32+f64"),
             "data": "synthetic",
             "config": {"workload": f"{n}^2 seeded random-rectangle deck, CG to 1e-10 relative residual, one "
                                    "timestep (halo, solve, solvefinished)", "n": n, "seed": DECK_SEED,
@@ -360,7 +369,9 @@ def gpu_arm(args):
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             # the solve's own launches plus the halo and solvefinished! kernels of each step
             "gpu_launches": int(sum(r.launches for r in hres) + 4 * len(hres)),
-            "variants": variants}
+            "variants": variants,
+            "vs_fp64_gpu": {k: variants["fp64"]["ms_per_step"] / v["ms_per_step"] for k, v in variants.items()
+                            if "ms_per_step" in v and "ms_per_step" in variants.get("fp64", {})}}
     if roof:
         dom = max(roof.values(), key=lambda d: d["ms"])
         dname = [k for k, v in roof.items() if v is dom][0]
@@ -530,7 +541,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--size", type=int, default=8192)
-    ap.add_argument("--variant", default="all", choices=["all", "fp64", "fp32_ir"])
+    ap.add_argument("--variant", default="all", choices=["all"] + list(VARIANTS))
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="timestep", choices=["timestep", "config2", "config4"],
                     help="timestep: the headline line; config2: the 4096^2 CG/Cheby/PPCG suite; "
