@@ -534,6 +534,84 @@ def run_config4(args):
     print(json.dumps(out))
 
 
+def conv_kernel_rates(tl, n, reps=10):
+    """Each convolution shape of the network (forward; and the input-gradient
+    mode) on one n x n image of random BF16 activations, timed with CUDA
+    events on torch's stream; FLOPs = 2 * 9 * cin * cout per pixel."""
+    import torch
+    lib = tl._abi.load()
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    out = {}
+    for ci, co, mode in ((16, 32, 1), (32, 32, 1), (32, 16, 0), (32, 32, 2)):
+        x = torch.randn((1, n, n, ci), device="cuda").to(torch.bfloat16)
+        w = (0.05 * torch.randn(co * 9 * ci, device="cuda")).to(torch.bfloat16)
+        b = torch.zeros(co, device="cuda")
+        y = torch.empty((1, n, n, co), device="cuda", dtype=torch.bfloat16)
+        gz = torch.randn((1, n, n, co), device="cuda").to(torch.bfloat16) if mode == 2 else None
+        g32 = torch.empty((1, n, n), device="cuda") if mode == 0 else None
+        args = (x.data_ptr(), w.data_ptr(), b.data_ptr() if mode != 2 else None,
+                gz.data_ptr() if gz is not None else None, None, y.data_ptr() if mode != 0 else None,
+                g32.data_ptr() if g32 is not None else None, 1, n, n, ci, co, mode, st)
+        for _ in range(2):
+            assert lib.tl_conv3x3_forward(*args) == 0
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            lib.tl_conv3x3_forward(*args)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        flops = 2.0 * 9 * ci * co * n * n
+        name = f"conv{ci}x{co}" + {0: "_out", 1: "_gelu", 2: "_input_grad"}[mode]
+        out[name] = {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12,
+                     "bytes": n * n * 2 * (ci + (co if mode else 2) + (co if mode == 2 else 0))}
+        out[name]["gbs"] = out[name]["bytes"] / (ms * 1e-3) / 1e9
+    return out
+
+
+def run_config5(args):
+    """The learned warm start: convolution kernel rates at n^2, one training
+    step (forward + residual loss + backward + Adam on 32 crops of 128^2) and
+    the A/B evaluation (plain start, network, extrapolation) on a held-out
+    random deck for FP64 CG and FP32 refinement."""
+    import torch
+    torch.cuda.set_device(0)
+    tl = load_package()
+    n = args.size if args.size != 8192 else 2048
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    bf16_peak = peaks.get("bf16_tflops", 1900.0)
+    rates = conv_kernel_rates(tl, n)
+    line = {"metric": "learned warm start: CG iterations and time to 1e-10 with and without the prediction",
+            "unit": "ms", "config": {"workload": f"{n}^2 held-out random-rectangle deck", "n": n,
+                                     "steps": args.steps, "seed": 900001},
+            "conv_kernels": rates, "bf16_peak_tflops": bf16_peak,
+            "conv_frac_of_bf16_peak": {k: v["tflops"] / bf16_peak for k, v in rates.items()}}
+    params = tl.warmstart.load_params()
+    traj = tl.warmstart.generate(tl, 512, [4242], 6)
+    pairs, scales = tl.warmstart._pairs(traj)
+    trn = tl.warmstart.Trainer(params, 32, 128, 128)
+    rng = np.random.default_rng(0)
+    for it in range(25):
+        if it == 5:
+            torch.cuda.synchronize()
+            t0 = time.time()
+        trn.step(tl.warmstart._random_crops(rng, traj, pairs, scales, 32, 128), 1e-6)
+    torch.cuda.synchronize()
+    line["train_step_ms"] = (time.time() - t0) * 1e3 / 20
+    if not args.no_eval:
+        ev = {}
+        for prec, pname in ((0, "fp64"), (1, "fp32_ir")):
+            r = tl.warmstart.evaluate(tl, params, n, 900001, args.steps, prec)
+            ev[pname] = {k: {"iters": sum(v["iters"]), "ms": sum(v["ms"]),
+                             "predictions_used": sum(1 for u in v["used"] if u == 1),
+                             "final_rel_diff": v.get("final_rel_diff"), "iters_per_step": v["iters"]}
+                         for k, v in r.items()}
+        line["eval"] = ev
+        line["value"] = ev["fp32_ir"]["network"]["ms"] / args.steps
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -543,9 +621,11 @@ def main():
     ap.add_argument("--size", type=int, default=8192)
     ap.add_argument("--variant", default="all", choices=["all"] + list(VARIANTS))
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="timestep", choices=["timestep", "config2", "config4"],
+    ap.add_argument("--workload", default="timestep", choices=["timestep", "config2", "config4", "config5"],
                     help="timestep: the headline line; config2: the 4096^2 CG/Cheby/PPCG suite; "
-                         "config4: 128 uneven decks, batched against sequential")
+                         "config4: 128 uneven decks, batched against sequential; config5: the learned warm "
+                         "start (kernel rates, training step, A/B evaluation; --size, --steps)")
+    ap.add_argument("--no-eval", action="store_true", help="config5: kernel rates and training step only")
     ap.add_argument("--decks", type=int, default=128)
     args = ap.parse_args()
     if args.warmup < 3:
@@ -554,6 +634,8 @@ def main():
         run_config2(args)
     elif args.workload == "config4":
         run_config4(args)
+    elif args.workload == "config5":
+        run_config5(args)
     elif args.impl == "reference":
         reference_arm(args)
     else:

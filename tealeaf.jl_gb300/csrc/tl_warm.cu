@@ -353,7 +353,9 @@ int tl_warm_try(tl_ctx *ctx, double rx, double ry, int warmstart, tl_result *res
 // from the plain start.  When a run's mean iteration count exceeds the mean of
 // its two controls, the prediction pauses for `backoff` steps (4, 8, ... 64)
 // and trust drops to 2; otherwise trust doubles (up to 32) and the backoff
-// returns to 4.
+// returns to 4.  A prediction rejected by the residual judge (outside a run)
+// pauses the next ones the same way, so that rejected inference stops
+// costing time.
 void tl_warm_after(tl_ctx *ctx, const tl_result *res) {
   tl_warm_state *ws = ctx->warm;
   if (!ws) return;
@@ -361,6 +363,12 @@ void tl_warm_after(tl_ctx *ctx, const tl_result *res) {
     ++ws->run;
     ws->run_iters += res->iters;
     return;
+  }
+  if (res->warm == 2 && ws->run == 0) {
+    // the prediction lost to the plain start by residual: its inference was
+    // wasted, so the next attempts back off the same way
+    ws->cooloff = ws->backoff;
+    ws->backoff = ws->backoff < 64 ? 2 * ws->backoff : 64;
   }
   if (ws->run > 0 && ws->ctrl_iters >= 0) {
     const double pred = (double)ws->run_iters / ws->run, plain = 0.5 * (ws->ctrl_iters + res->iters);

@@ -183,7 +183,8 @@ def test_warm_start_judge_and_accuracy(tl, built_lib, precision):
         assert w["used"][0] == 0                       # no previous step yet
         # the guard, restated: runs of at most `trust` solves from the
         # prediction between plain-start controls; a run that needed more
-        # iterations than the mean of its two controls pauses the prediction
+        # iterations than the mean of its two controls, or a rejected
+        # prediction, pauses the prediction
         ctrl, run, run_iters, trust, cooloff, backoff = w["iters"][0], 0, 0, 2, 0, 4
         for k in range(1, 12):
             used, a, b, it = w["used"][k], w["r0_pred"][k], w["r0_plain"][k], w["iters"][k]
@@ -198,6 +199,8 @@ def test_warm_start_judge_and_accuracy(tl, built_lib, precision):
             if used == 1:
                 run, run_iters = run + 1, run_iters + it
                 continue
+            if used == 2 and run == 0:
+                cooloff, backoff = backoff, min(2 * backoff, 64)
             if run:
                 if run_iters / run > 0.5 * (ctrl + it):
                     cooloff, backoff, trust = backoff, min(2 * backoff, 64), 2
