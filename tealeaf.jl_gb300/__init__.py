@@ -387,18 +387,38 @@ def debugrecord(settings: Settings, chunk: Chunk):
 
 
 def _julia_repr(v: float) -> str:
-    """Julia's shortest round-trip print of a Float64."""
+    """Julia's `print` of a Float64: the shortest round-trip digits (the same
+    digits Python's repr finds), written in fixed form when the decimal point
+    falls at -4 < pt <= 6 digits from the first digit (and the value is not an
+    integer whose exact value differs from its shortest digits), otherwise as
+    d.ddde<exp>."""
+    import decimal
+    import math
+    v = float(v)
     if v != v:
         return "NaN"
-    if v in (float("inf"), float("-inf")):
+    if math.isinf(v):
         return "Inf" if v > 0 else "-Inf"
-    r = repr(float(v))
-    if "e" in r:
-        mant, ex = r.split("e")
-        if "." not in mant:
-            mant += ".0"
-        return f"{mant}e{int(ex)}"
-    return r
+    sign = "-" if math.copysign(1.0, v) < 0 else ""
+    if v == 0:
+        return sign + "0.0"
+    t = decimal.Decimal(repr(abs(v))).normalize().as_tuple()
+    digits = "".join(str(d) for d in t.digits)
+    olength = len(digits)
+    pt = t.exponent + olength
+    fixed = -4 < pt <= 6
+    if fixed and pt >= olength:
+        fixed = not abs(math.fmod(abs(v) + 0.05, 10.0 ** (pt - olength)) - 0.05) > 0.05
+    if fixed:
+        if pt <= 0:
+            body = "0." + "0" * (-pt) + digits
+        elif pt >= olength:
+            body = digits + "0" * (pt - olength) + ".0"
+        else:
+            body = digits[:pt] + "." + digits[pt:]
+    else:
+        body = digits[0] + "." + (digits[1:] or "0") + "e" + str(pt - 1)
+    return sign + body
 
 
 from . import warmstart  # noqa: E402  (learned warm start: network file, training, evaluation)

@@ -139,3 +139,59 @@ def test_coefficient_error(tl, built_lib):
     with pytest.raises(tl.TeaLeafError) as e:
         tl.CG.solve(chunk, s, 0.004, 0.004)
     assert e.value.code == 3
+
+
+GEOMETRY_DECK = """state 1 density=100.0 energy=0.0001
+state 2 density=0.5 energy=20.0 geometry=circular xmin=4.0 ymin=5.0 radius=2.2
+state 3 density=2.0 energy=5.0 geometry=rectangle xmin=6.0 xmax=9.0 ymin=1.0 ymax=3.0
+state 4 density=1.5 energy=8.0 geometry=point xmin=2.5 ymin=7.5
+x_cells=32
+y_cells=32
+xmin=0.0
+ymin=0.0
+xmax=10.0
+ymax=10.0
+initial_timestep=0.004
+end_step=2
+max_iters=5000
+use_cg
+eps=1e-12
+halo_depth=2
+coefficient=1
+summary_frequency=10
+"""
+
+
+@pytest.mark.parametrize("mode", [REF, TEA])
+def test_circular_and_point_states(tl, built_lib, mode):
+    """setchunkstate! with circular and point states (chunk.jl:138-140; in
+    reference mode every state takes the rectangle arm), then two CG steps:
+    bit-identical to the oracle in device order."""
+    chunk, res, sums, per = gpu_run(tl, GEOMETRY_DECK, mode, exact=True, steps_fields=True)
+    _, ores, osums, oper = oracle_run(GEOMETRY_DECK, mode, O.ORDER_DEVICE, _layout(chunk), steps_fields=True)
+    assert [r.iters for r in res] == [r.iters for r in ores]
+    for f in FIELDS:
+        np.testing.assert_array_equal(per[-1][f], oper[-1][f], err_msg=f)
+    if mode == TEA:
+        assert np.any(chunk.field("density") == 0.5)    # the circle was drawn
+
+
+def test_debugrecord_dump(tl, built_lib, tmp_path):
+    """debugrecord (src/TeaLeaf.jl:90-107): each field's name, then each column
+    of the (X, Y) array on one line, then a blank line; the printed values
+    read back to the device values exactly."""
+    s = tl.Settings.from_text(CONFIG1, mode=TEA)
+    chunk = tl.initialiseapp(s)
+    s.debugfile = str(tmp_path / "dump.txt")
+    tl.debugrecord(s, chunk)
+    lines = (tmp_path / "dump.txt").read_text().split("\n")
+    X, Y = chunk.size()
+    pos = 0
+    for name in tl._CHUNK_DUMP_FIELDS:
+        assert lines[pos] == name
+        a = chunk.field(name)
+        for j in range(Y):
+            vals = [float(t) for t in lines[pos + 1 + j].split(" ")]
+            assert vals == list(a[:, j])
+        assert lines[pos + 1 + Y] == ""
+        pos += Y + 2

@@ -96,3 +96,13 @@ def test_library_loads_through_binding(built_lib):
     assert lib.tl_destroy(None) == 0
     ctx = C.c_void_p()
     assert lib.tl_create(C.byref(ctx), None) == 1       # null configuration: rejected before any CUDA call
+
+
+@pytest.mark.parametrize("v,text", [(1.0, "1.0"), (0.5, "0.5"), (0.1, "0.1"), (100000.0, "100000.0"),
+                                    (1e6, "1.0e6"), (1234567.0, "1.234567e6"), (0.0001, "0.0001"),
+                                    (1e-5, "1.0e-5"), (2.5e-7, "2.5e-7"), (-3.25, "-3.25"), (123.456, "123.456"),
+                                    (0.0, "0.0"), (-0.0, "-0.0"), (1e16, "1.0e16"), (120000.0, "120000.0"),
+                                    (0.00012, "0.00012"), (float("nan"), "NaN"), (float("-inf"), "-Inf")])
+def test_julia_float_print(tl, v, text):
+    """debugrecord writes floats the way Julia's print does (src/TeaLeaf.jl:90-107)."""
+    assert tl._julia_repr(v) == text
