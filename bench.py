@@ -489,17 +489,26 @@ def config4_decks(count: int = 128, seed: int = DECK_SEED + 4):
 
 def run_config4(args):
     """128 independent decks of uneven sizes, 10 timesteps each, CG to 1e-10
-    relative residual: one batched graph launch per timestep against the same
-    decks solved one after another by the single-deck fused CG."""
+    relative residual, FP64 and FP32-refined: one batched graph launch per
+    timestep against the same decks solved one after another by the
+    single-deck solver of the same precision."""
     import torch
     torch.cuda.set_device(0)
     tl = load_package()
     sizes, texts = config4_decks(args.decks)
     steps = 10
     out = {"workload": f"config4: {len(texts)} random-rectangle decks, nx, ny in 256..2048 step 128, {steps} steps, "
-                       "CG to 1e-10 relative (recursive residual)", "cells": sum(a * b for a, b in sizes)}
+                       "CG to 1e-10 relative", "cells": sum(a * b for a, b in sizes)}
+    for prec, pname in ((0, "fp64"), (1, "fp32_ir")):
+        out[pname] = run_config4_precision(tl, texts, steps, prec)
+        out[pname]["speedup"] = out[pname]["sequential"]["seconds"] / out[pname]["batched"]["seconds"]
+    print(json.dumps(out))
+
+
+def run_config4_precision(tl, texts, steps, precision):
+    out = {}
     for mode in ("batched", "sequential"):
-        sets = [tl.Settings.from_text(t, mode=1, criterion=1) for t in texts]
+        sets = [tl.Settings.from_text(t, mode=1, criterion=1, precision=precision) for t in texts]
         chunks = [tl.initialiseapp(s) for s in sets]
         lib = chunks[0].lib
         for c in chunks:
@@ -530,8 +539,7 @@ def run_config4(args):
         out[mode] = {"seconds": wall, "iterations": iters, "temp_summaries_first4": summ[:4]}
         for c in chunks:
             c.close()
-    out["speedup"] = out["sequential"]["seconds"] / out["batched"]["seconds"]
-    print(json.dumps(out))
+    return out
 
 
 def conv_kernel_rates(tl, n, reps=10):

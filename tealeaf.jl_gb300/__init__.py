@@ -325,14 +325,15 @@ class Batch:
 
     def solve(self, settings_list) -> List[SolveResult]:
         """CG.solve!(chunk, set, rx, ry) for every deck at once; the solver
-        parameters (eps, maxiters, coefficient, criterion) come from the first
-        deck's settings, rx/ry from each deck's own."""
+        parameters (eps, maxiters, coefficient, criterion, precision: FP64 or
+        FP32-refined) come from the first deck's settings, rx/ry from each
+        deck's own."""
         n = len(self.chunks)
         rx = (C.c_double * n)(*[s.dtinit / s.dx ** 2 for s in settings_list])
         ry = (C.c_double * n)(*[s.dtinit / s.dy ** 2 for s in settings_list])
         prm = _params(settings_list[0], _abi.SOLVER_CG)
         prm.exact = 0
-        prm.precision = _abi.PREC_FP64
+        prm.warmstart = 0
         res = (_abi.Result * n)()
         rc = self.lib.tl_batch_solve(self._b, rx, ry, C.byref(prm), res)
         if rc:

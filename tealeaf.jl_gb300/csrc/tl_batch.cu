@@ -11,12 +11,19 @@
 // deck's blocks return at once (the per-deck convergence mask), and at the end
 // of every two-iteration loop body the map is rebuilt over the decks still
 // running, which also sets the while-node's condition.
+//
+// With FP32 refinement the body runs two FP32 inner iterations for the decks
+// in their inner loop, then the FP64 refinement step (u += x, halo of u, true
+// residual, test) for the decks whose inner loop just ended; the test either
+// finishes the deck or restarts its inner loop from the true residual, all on
+// the device.
 #include <cstdio>
 #include <cstring>
 #include <new>
 #include <vector>
 
 #include "tl_cg_ops.cuh"
+#include "tl_ir_ops.cuh"
 #include "tl_solvers.h"
 
 namespace tl {
@@ -31,6 +38,11 @@ struct DeckDesc {
   Geom g;
   int ntx, tiles;
   long long cells;
+  // FP32 refinement buffers (filled on the first batched FP32 solve)
+  G32 g32;
+  IrPtrs q;
+  float *p32, *pb32;
+  int ntx32, tiles32;
 };
 
 struct BatchMap {
@@ -155,6 +167,169 @@ __global__ void __launch_bounds__(256) k_batch_ur(const DeckDesc *decks, const B
   finish_deck<1>(acc, op, nb, lb);
 }
 
+// ---- FP32 refinement --------------------------------------------------------
+
+// Walk with four cells per lane: tiles of 128*BATCH_WARPS columns x BATCH_ROWS rows.
+template <class Op>
+__device__ __forceinline__ void walk_deck32(const DeckDesc &D, const Op &op, int lb, int nblocks, double (&acc)[1]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int TW = 128 * BATCH_WARPS;
+  for (int t = lb; t < D.tiles32; t += nblocks) {
+    const int tx = t % D.ntx32, ty = t / D.ntx32;
+    const int i0 = tx * TW + warp * 128 + 4 * lane;
+    const int j0 = ty * BATCH_ROWS;
+    const int j1 = min(j0 + BATCH_ROWS, D.g.ny);
+    op.tile(i0, j0, j1, acc);
+  }
+}
+
+// FP32 W step of every deck in its inner loop: p' = beta p + r, w = A p', p'.w.
+__global__ void __launch_bounds__(256) k_batch_ir_w(const DeckDesc *decks, const BatchMap *map, int parity) {
+  const int d = find_deck(map->first_w, map->nblk_w, map->n, blockIdx.x);
+  if (d < 0) return;
+  const DeckDesc &D = decks[d];
+  if (D.F.sc->done) return;
+  OpIrW op;
+  op.F = D.F;
+  op.g = D.g32;
+  op.q = D.q;
+  op.psrc = parity ? D.pb32 : D.p32;
+  op.pdst = parity ? D.p32 : D.pb32;
+  op.guard = 0;
+  double acc[1] = {0.0};
+  const int lb = blockIdx.x - map->first_w[d], nb = map->nblk_w[d];
+  walk_deck32(D, op, lb, nb, acc);
+  finish_deck<1>(acc, op, nb, lb);
+}
+
+// The FP32 u/r step's epilogue, plus where the search direction ended: after
+// the even step it is in the second buffer.
+struct OpIrURBatch : OpIrUR {
+  int parity;
+  __device__ void fin(const double *tot) const {
+    OpIrUR::fin(tot);
+    if (F.sc->done) F.sc->pbuf = parity == 0 ? 1 : 0;
+  }
+};
+
+// FP32 UR step: x += alpha p', r -= alpha w, r.r, beta, and the refinement test.
+__global__ void __launch_bounds__(256) k_batch_ir_ur(const DeckDesc *decks, const BatchMap *map, int parity) {
+  const int d = find_deck(map->first_u, map->nblk_u, map->n, blockIdx.x);
+  if (d < 0) return;
+  const DeckDesc &D = decks[d];
+  if (D.F.sc->done) return;
+  OpIrURBatch op;
+  op.F = D.F;
+  op.g = D.g32;
+  op.q = D.q;
+  op.p = parity ? D.p32 : D.pb32;
+  op.guard = 0;
+  op.cond = 0;
+  op.set_cond = 0;
+  op.parity = parity;
+  double acc[1] = {0.0};
+  const int lb = blockIdx.x - map->first_u[d], nb = map->nblk_u[d];
+  walk_deck32(D, op, lb, nb, acc);
+  finish_deck<1>(acc, op, nb, lb);
+}
+
+// A deck whose inner loop has ended and whose solve is not over.
+__device__ __forceinline__ bool refining(const DeckDesc &D) { return D.F.sc->done && !D.F.sc->finished; }
+
+// Refinement, FP64: u += x, x = 0; the current search direction moves to the
+// first buffer.
+__global__ void k_batch_ir_fold(const DeckDesc *decks, const BatchMap *map) {
+  const int d = find_deck(map->first_w, map->nblk_w, map->n, blockIdx.x);
+  if (d < 0) return;
+  const DeckDesc &D = decks[d];
+  if (!refining(D)) return;
+  const int lb = blockIdx.x - map->first_w[d], nb = map->nblk_w[d];
+  const bool move = D.F.sc->pbuf != 0;
+  const long long n = (long long)D.g.nx * D.g.ny;
+  for (long long k = (long long)lb * blockDim.x + threadIdx.x; k < n; k += (long long)nb * blockDim.x) {
+    const int i = (int)(k % D.g.nx), j = (int)(k / D.g.nx);
+    const size_t c = D.g.at(i, j), c32 = D.g32.at(i, j);
+    D.F.u[c] = D.F.u[c] + (double)D.q.x[c32];
+    D.q.x[c32] = 0.f;
+    if (move) D.p32[c32] = D.pb32[c32];
+  }
+}
+
+// Refinement: the reflective halo of u, depth 1, faces only (corners untouched).
+__global__ void k_batch_ir_halo(const DeckDesc *decks, const BatchMap *map) {
+  const int d = find_deck(map->first_w, map->nblk_w, map->n, blockIdx.x);
+  if (d < 0) return;
+  const DeckDesc &D = decks[d];
+  if (!refining(D)) return;
+  const int lb = blockIdx.x - map->first_w[d], nb = map->nblk_w[d];
+  const int nx = D.g.nx, ny = D.g.ny;
+  double *u = D.F.u;
+  for (int k = lb * blockDim.x + threadIdx.x; k < 2 * (nx + ny); k += nb * blockDim.x) {
+    if (k < ny) u[D.g.at(-1, k)] = u[D.g.at(0, k)];
+    else if (k < 2 * ny) u[D.g.at(nx, k - ny)] = u[D.g.at(nx - 1, k - ny)];
+    else if (k < 2 * ny + nx) u[D.g.at(k - 2 * ny, -1)] = u[D.g.at(k - 2 * ny, 0)];
+    else u[D.g.at(k - 2 * ny - nx, ny)] = u[D.g.at(k - 2 * ny - nx, ny - 1)];
+  }
+}
+
+// Refinement: the true residual r = u0 - A u (FP64), r32 = (float) r, and the
+// test: the deck finishes (converged, or out of iterations) or its inner loop
+// restarts from the true residual with the search direction kept.
+struct OpIrResidBatch : OpIrResid {
+  __device__ void fin(const double *tot) const {
+    DevScalars *sc = F.sc;
+    const double rr = tot[0];
+    const double rel = sc->bb > 0 ? sqrt(rr / sc->bb) : sqrt(rr);
+    sc->red[0] = rr;
+    sc->red[1] = rel;
+    sc->refinements += 1;
+    if (rel < sc->eps || sc->iter >= sc->maxiters) {
+      sc->finished = 1;
+      sc->converged = rel < sc->eps;
+    } else {
+      sc->rro = rr;
+      sc->rr_ref = rr;
+      sc->done = 0;
+      sc->switched = 0;
+      sc->pbuf = 0;
+    }
+  }
+};
+
+__global__ void __launch_bounds__(256) k_batch_ir_resid(const DeckDesc *decks, const BatchMap *map) {
+  const int d = find_deck(map->first_w, map->nblk_w, map->n, blockIdx.x);
+  if (d < 0) return;
+  const DeckDesc &D = decks[d];
+  if (!refining(D)) return;
+  OpIrResidBatch op;
+  op.F = D.F;
+  op.g = D.g;
+  op.g32 = D.g32;
+  op.r32 = D.q.r;
+  double acc[1] = {0.0};
+  const int lb = blockIdx.x - map->first_w[d], nb = map->nblk_w[d];
+  walk_deck(D, op, lb, nb, acc);
+  finish_deck<1>(acc, op, nb, lb);
+}
+
+// Start of a deck's FP32-refined solve (after tea_leaf_init, copyu! and the
+// FP32 copies): the first refinement reference and the initial test.
+__global__ void k_batch_ir_start(DevScalars *sc, double delta2) {
+  const double rr = sc->rro;
+  const double rel = sc->bb > 0 ? sqrt(rr / sc->bb) : sqrt(rr);
+  sc->rr_ref = rr;
+  sc->delta2 = delta2;
+  sc->switched = 0;
+  sc->pbuf = 0;
+  sc->refinements = 0;
+  sc->red[0] = rr;
+  sc->red[1] = rel;
+  const int fin = rel < sc->eps || sc->maxiters < 1;
+  sc->finished = fin;
+  sc->done = fin;
+  sc->converged = rel < sc->eps;
+}
+
 // Shares `total` blocks over the unconverged decks in proportion to their
 // cells: one each, the rest in proportion (rounded down), at most one block
 // per tile.
@@ -196,15 +371,17 @@ __device__ void share(const DeckDesc *decks, BatchMap *map, const int *act, int 
 }
 
 // Rebuilds the block map over the decks still running and sets the loop
-// condition (any deck left).
-__global__ void k_batch_map(const DeckDesc *decks, BatchMap *map, cudaGraphConditionalHandle cond, int set_cond) {
+// condition (any deck left).  A deck runs until `done` (FP64) or `finished`
+// (FP32 refinement, where `done` only ends an inner loop).
+__global__ void k_batch_map(const DeckDesc *decks, BatchMap *map, cudaGraphConditionalHandle cond, int set_cond,
+                            int ir) {
   __shared__ int act[BATCH_MAX];
   __shared__ int nact;
   const int n = map->n;
   if (threadIdx.x == 0) nact = 0;
   __syncthreads();
   for (int d = threadIdx.x; d < n; d += blockDim.x) {
-    act[d] = decks[d].F.sc->done ? 0 : 1;
+    act[d] = (ir ? decks[d].F.sc->finished : decks[d].F.sc->done) ? 0 : 1;
     if (act[d]) atomicAdd(&nact, 1);
   }
   __syncthreads();
@@ -230,7 +407,10 @@ struct tl_batch {
   BatchMap *d_map = nullptr;
   BatchMap *h_map = nullptr;
   int total_w = 0, total_u = 0;
-  cudaGraphExec_t graph = nullptr;
+  cudaGraphExec_t graph = nullptr;     // FP64 CG loop
+  cudaGraphExec_t graph_ir = nullptr;  // FP32-refined CG loop
+  int ir_ready = 0;                    // the deck table holds the FP32 buffers
+  std::vector<DeckDesc> h_decks;
   double last_ms = 0.0;
   char msg[512] = {};
 };
@@ -247,7 +427,7 @@ int bfail(tl_batch *b, cudaError_t e, const char *what) {
     if (e_ != cudaSuccess) return bfail(b, e_, #x); \
   } while (0)
 
-int build_graph(tl_batch *b) {
+int build_graph(tl_batch *b, int ir) {
   cudaGraph_t graph = nullptr;
   BCK(cudaGraphCreate(&graph, 0));
   cudaGraphConditionalHandle h;
@@ -274,10 +454,20 @@ int build_graph(tl_batch *b) {
     return bfail(b, e, "cudaStreamBeginCaptureToGraph");
   }
   for (int parity = 0; parity < 2; ++parity) {
-    k_batch_w<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
-    k_batch_ur<<<b->total_u, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
+    if (ir) {
+      k_batch_ir_w<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
+      k_batch_ir_ur<<<b->total_u, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
+    } else {
+      k_batch_w<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
+      k_batch_ur<<<b->total_u, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
+    }
   }
-  k_batch_map<<<1, 256, 0, b->stream>>>(b->d_decks, b->d_map, h, 1);
+  if (ir) {
+    k_batch_ir_fold<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map);
+    k_batch_ir_halo<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map);
+    k_batch_ir_resid<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map);
+  }
+  k_batch_map<<<1, 256, 0, b->stream>>>(b->d_decks, b->d_map, h, 1, ir);
   cudaError_t le = cudaGetLastError();
   cudaGraph_t captured = nullptr;
   e = cudaStreamEndCapture(b->stream, &captured);
@@ -285,7 +475,7 @@ int build_graph(tl_batch *b) {
     cudaGraphDestroy(graph);
     return bfail(b, e != cudaSuccess ? e : le, "capture of the batch loop");
   }
-  e = cudaGraphInstantiate(&b->graph, graph, 0);
+  e = cudaGraphInstantiate(ir ? &b->graph_ir : &b->graph, graph, 0);
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) return bfail(b, e, "cudaGraphInstantiate");
   return TL_OK;
@@ -347,6 +537,7 @@ extern "C" int tl_batch_create(tl_batch **out, tl_ctx *const *ctxs, int n) {
   b->h_map->total_w = b->total_w;
   b->h_map->total_u = b->total_u;
   BCK(cudaMemcpyAsync(b->d_decks, h.data(), sizeof(DeckDesc) * n, cudaMemcpyHostToDevice, b->stream));
+  b->h_decks = h;
   BCK(cudaMemcpyAsync(b->d_map, b->h_map, sizeof(BatchMap), cudaMemcpyHostToDevice, b->stream));
   BCK(cudaStreamSynchronize(b->stream));
   return TL_OK;
@@ -356,6 +547,7 @@ extern "C" int tl_batch_destroy(tl_batch *b) {
   if (!b) return TL_OK;
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->graph_ir) cudaGraphExecDestroy(b->graph_ir);
   if (b->d_decks) cudaFree(b->d_decks);
   if (b->d_map) cudaFree(b->d_map);
   if (b->h_map) cudaFreeHost(b->h_map);
@@ -368,13 +560,138 @@ extern "C" int tl_batch_destroy(tl_batch *b) {
 
 extern "C" const char *tl_batch_last_error(const tl_batch *b) { return b ? b->msg : "null batch"; }
 
+namespace {
+
+int grid_cells_of(const Geom &g, int full) {
+  long long n = full ? (long long)g.X * g.Y : (long long)g.nx * g.ny;
+  long long blocks = (n + 255) / 256;
+  if (blocks > 152LL * 32) blocks = 152LL * 32;
+  return (int)(blocks < 1 ? 1 : blocks);
+}
+
+// The FP32-refined batch: per deck tea_leaf_init (reference operation order),
+// copyu!, the FP32 copies and the first test; one graph launch for the
+// inner iterations and refinements of every deck; per deck the last search
+// direction back to FP64 and the halo of u, p.
+int batch_solve_ir(tl_batch *b, const double *rx, const double *ry, const tl_params *prm, tl_result *results) {
+  const int n = (int)b->ctx.size();
+  for (int k = 0; k < n; ++k) {
+    tl_ctx *ctx = b->ctx[k];
+    if (!ctx->initialised || prm->maxiters > ctx->cfg.maxiters) {
+      snprintf(b->msg, sizeof b->msg, "deck %d: not initialised, or maxiters beyond its tables", k);
+      return TL_ERR_STATE;
+    }
+    const int rc = tl_ensure_ir(ctx);
+    if (rc) {
+      snprintf(b->msg, sizeof b->msg, "deck %d: %s", k, ctx->msg);
+      return rc;
+    }
+  }
+  if (!b->ir_ready) {
+    for (int k = 0; k < n; ++k) {
+      tl_ctx *ctx = b->ctx[k];
+      DeckDesc &D = b->h_decks[k];
+      D.g32.nx = ctx->g.nx;
+      D.g32.ny = ctx->g.ny;
+      D.g32.hd = ctx->g.hd;
+      D.g32.X = ctx->g.X;
+      D.g32.Y = ctx->g.Y;
+      D.g32.pitch = ctx->ir->pitch;
+      D.q.kx = ctx->ir->kx;
+      D.q.ky = ctx->ir->ky;
+      D.q.r = ctx->ir->r;
+      D.q.w = ctx->ir->w;
+      D.q.x = ctx->ir->x;
+      D.p32 = ctx->ir->p;
+      D.pb32 = ctx->ir->pb;
+      D.ntx32 = (ctx->g.nx + 128 * BATCH_WARPS - 1) / (128 * BATCH_WARPS);
+      D.tiles32 = D.ntx32 * ((ctx->g.ny + BATCH_ROWS - 1) / BATCH_ROWS);
+    }
+    BCK(cudaMemcpyAsync(b->d_decks, b->h_decks.data(), sizeof(DeckDesc) * n, cudaMemcpyHostToDevice, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    b->ir_ready = 1;
+  }
+  std::vector<cudaStream_t> own(n);
+  for (int k = 0; k < n; ++k) {
+    own[k] = b->ctx[k]->stream;
+    b->ctx[k]->stream = b->stream;
+  }
+  auto restore = [&]() {
+    for (int k = 0; k < n; ++k) b->ctx[k]->stream = own[k];
+  };
+  tl_params p = *prm;
+  p.criterion = TL_CRIT_RELATIVE;
+  int rc = TL_OK;
+  for (int k = 0; k < n && !rc; ++k) {
+    tl_ctx *ctx = b->ctx[k];
+    const DeckDesc &D = b->h_decks[k];
+    memset(&results[k], 0, sizeof(tl_result));
+    results[k].r0_plain = results[k].r0_pred = -1.0;
+    ctx->launches = 0;
+    rc = tl_cg_init(ctx, rx[k], ry[k], p.coefficient, 1);
+    if (!rc) rc = tl_set_loop_params(ctx, &p, 0, 0);
+    const int up[2] = {TL_EX_U, TL_EX_P};
+    if (!rc) rc = tl_halo_update(ctx, 1, up, 2, 1);
+    if (!rc) rc = tl_copy_u(ctx);
+    if (!rc) {
+      k_ir_convert<<<grid_cells_of(ctx->g, 1), 256, 0, b->stream>>>(ctx->F, ctx->g, D.g32, D.q.kx, D.q.ky, D.q.r,
+                                                                    D.p32, D.q.x);
+      k_batch_ir_start<<<1, 1, 0, b->stream>>>(ctx->F.sc, IR_DELTA * IR_DELTA);
+      if (cudaGetLastError() != cudaSuccess) rc = TL_ERR_CUDA;
+    }
+    if (rc) snprintf(b->msg, sizeof b->msg, "deck %d: %s", k, ctx->msg);
+  }
+  if (rc) {
+    restore();
+    return rc;
+  }
+  k_batch_map<<<1, 256, 0, b->stream>>>(b->d_decks, b->d_map, 0, 0, 1);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && !b->graph_ir) rc = build_graph(b, 1);
+  if (e == cudaSuccess && !rc) e = cudaEventRecord(b->ev0, b->stream);
+  if (e == cudaSuccess && !rc) e = cudaGraphLaunch(b->graph_ir, b->stream);
+  if (e == cudaSuccess && !rc) e = cudaEventRecord(b->ev1, b->stream);
+  if (e == cudaSuccess && !rc) e = cudaEventSynchronize(b->ev1);
+  float ms = 0.f;
+  if (e == cudaSuccess && !rc) e = cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+  b->last_ms = ms;
+  if (e != cudaSuccess) rc = bfail(b, e, "FP32-refined batch loop");
+  for (int k = 0; k < n && !rc; ++k) {
+    tl_ctx *ctx = b->ctx[k];
+    const DeckDesc &D = b->h_decks[k];
+    k_ir_export_p<<<grid_cells_of(ctx->g, 0), 256, 0, b->stream>>>(ctx->F, ctx->g, D.g32, D.p32);
+    const int up[2] = {TL_EX_U, TL_EX_P};
+    rc = tl_halo_update(ctx, 1, up, 2, 1);
+    if (!rc) rc = tl_read_scalars(ctx);
+    if (rc) break;
+    const DevScalars &sc = *ctx->host_sc;
+    results[k].iters = sc.iter;
+    results[k].cg_iters = sc.iter;
+    results[k].error = sc.red[0];
+    results[k].rel_residual = sc.red[1];
+    results[k].converged = sc.converged;
+    results[k].refinements = sc.refinements;
+    results[k].launches = 0;
+  }
+  if (!rc) {
+    e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) rc = bfail(b, e, "batch epilogue");
+  }
+  restore();
+  return rc;
+}
+
+}  // namespace
+
 extern "C" int tl_batch_solve(tl_batch *b, const double *rx, const double *ry, const tl_params *prm,
                               tl_result *results) {
   if (!b || !rx || !ry || !prm || !results) return TL_ERR_ARG;
-  if (prm->solver != TL_SOLVER_CG || prm->precision != TL_PREC_FP64 || prm->exact) {
-    snprintf(b->msg, sizeof b->msg, "batched solves run the fused FP64 CG (solver CG, FP64, exact 0)");
+  if (prm->solver != TL_SOLVER_CG || prm->exact ||
+      (prm->precision != TL_PREC_FP64 && prm->precision != TL_PREC_FP32_IR)) {
+    snprintf(b->msg, sizeof b->msg, "batched solves run CG (fused FP64 or FP32-refined, exact 0)");
     return TL_ERR_ARG;
   }
+  if (prm->precision == TL_PREC_FP32_IR) return batch_solve_ir(b, rx, ry, prm, results);
   const int n = (int)b->ctx.size();
   // each deck's CG.init!, halo of u, p and copyu, on the batch stream
   std::vector<cudaStream_t> own(n);
@@ -407,9 +724,9 @@ extern "C" int tl_batch_solve(tl_batch *b, const double *rx, const double *ry, c
     return rc;
   }
   if (prm->maxiters >= 1) {
-    k_batch_map<<<1, 256, 0, b->stream>>>(b->d_decks, b->d_map, 0, 0);
+    k_batch_map<<<1, 256, 0, b->stream>>>(b->d_decks, b->d_map, 0, 0, 0);
     cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess && !b->graph) rc = build_graph(b);
+    if (e == cudaSuccess && !b->graph) rc = build_graph(b, 0);
     if (e == cudaSuccess && !rc) e = cudaEventRecord(b->ev0, b->stream);
     if (e == cudaSuccess && !rc) e = cudaGraphLaunch(b->graph, b->stream);
     if (e == cudaSuccess && !rc) e = cudaEventRecord(b->ev1, b->stream);

@@ -59,6 +59,10 @@ struct DevScalars {
   int first;            // the next fused CG step starts from p itself (no beta update)
   double rr_ref;        // FP32 refinement: r.r at the last refinement
   double delta2;        // FP32 refinement: refine once r.r < delta2 * rr_ref
+  // batched FP32 refinement (tl_batch.cu)
+  int pbuf;             // 1: the current FP32 search direction is in the second buffer
+  int finished;         // the deck's solve is over (converged or out of iterations)
+  int refinements;      // FP64 refinement steps taken
 };
 
 // Device pointers of one context, passed to kernels by value.

@@ -47,3 +47,30 @@ def test_batch_rejects_reference_mode(tl, built_lib):
     c = tl.initialiseapp(s)
     with pytest.raises(tl.TeaLeafError):
         tl.Batch([c])
+
+
+def test_batch_fp32_refined_matches_single_solves(tl, built_lib):
+    """FP32 inner sweeps with FP64 refinement, batched: every deck meets the
+    1e-10 relative true residual; iteration counts within 5 % of the deck's
+    own FP32-refined solve (the FP32 sums differ in rounding, which moves the
+    refinement points); u within 1e-8 of its maximum."""
+    texts = _decks()
+    kw = dict(mode=1, criterion=1, precision=1)
+    sets = [tl.Settings.from_text(t, **kw) for t in texts]
+    chunks = [tl.initialiseapp(s) for s in sets]
+    hist = tl.diffuse_batch(chunks, sets, steps=3)
+    for k, t in enumerate(texts):
+        s1 = tl.Settings.from_text(t, **kw)
+        c1 = tl.initialiseapp(s1)
+        single = []
+        for _ in range(3):
+            tl.haloupdate(c1, s1, 1, ["energy", "density"])
+            single.append(tl.CG.solve(c1, s1, s1.dtinit / s1.dx ** 2, s1.dtinit / s1.dy ** 2))
+            tl.solvefinished(c1, s1)
+        for step in range(3):
+            b, o = hist[step][k], single[step]
+            assert b.converged and 0 <= b.rel_residual < 1e-10, (k, step, b)
+            assert b.refinements >= 1
+            assert abs(b.iters - o.iters) <= max(3, 0.05 * o.iters), (k, step, b.iters, o.iters)
+        u, ou = chunks[k].field("u"), c1.field("u")
+        assert np.max(np.abs(u - ou)) <= 1e-8 * np.max(np.abs(ou))
