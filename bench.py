@@ -514,29 +514,36 @@ def run_config4_precision(tl, texts, steps, precision):
         for c in chunks:
             c.check(lib.tl_synchronize(c.ctx))
         t0 = time.perf_counter()
-        iters = 0
+        iters, loop_ms, first_loop_ms = 0, 0.0, 0.0
         if mode == "batched":
             batch = tl.Batch(chunks)
-            for _ in range(steps):
+            for step in range(steps):
                 for c, s in zip(chunks, sets):
                     tl.haloupdate(c, s, 1, ["energy", "density"])
                 res = batch.solve(sets)
                 iters += sum(r.iters for r in res)
+                loop_ms += res[0].solve_ms
+                if step == 0:
+                    first_loop_ms = res[0].solve_ms
                 for c, s in zip(chunks, sets):
                     tl.solvefinished(c, s)
             batch.close()
         else:
             for c, s in zip(chunks, sets):
-                for _ in range(steps):
+                for step in range(steps):
                     tl.haloupdate(c, s, 1, ["energy", "density"])
                     r = tl.CG.solve(c, s, s.dtinit / s.dx ** 2, s.dtinit / s.dy ** 2)
                     iters += r.iters
+                    loop_ms += r.solve_ms
+                    if step == 0:
+                        first_loop_ms += r.solve_ms
                     tl.solvefinished(c, s)
         for c in chunks:
             c.check(lib.tl_synchronize(c.ctx))
         wall = time.perf_counter() - t0
         summ = [tl.fieldsummary(c, s, problemfile=None)[3] for c, s in zip(chunks, sets)]
-        out[mode] = {"seconds": wall, "iterations": iters, "temp_summaries_first4": summ[:4]}
+        out[mode] = {"seconds": wall, "iterations": iters, "loop_ms": loop_ms, "first_step_loop_ms": first_loop_ms,
+                     "temp_summaries_first4": summ[:4]}
         for c in chunks:
             c.close()
     return out
