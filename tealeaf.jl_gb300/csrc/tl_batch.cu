@@ -33,16 +33,20 @@ constexpr int BATCH_MAX = 1024;  // decks per batch
 constexpr int BATCH_WARPS = 8;
 constexpr int BATCH_ROWS = 8;
 
+// Work is handed out per warp: a warp tile is one warp's column strip (64
+// columns for the FP64 kernels, 128 for the FP32 ones) over BATCH_ROWS rows,
+// and the warps of a deck's blocks take its warp tiles in turn.  Narrow decks
+// then keep every warp busy.
 struct DeckDesc {
   Fields F;
   Geom g;
-  int ntx, tiles;
+  int ntx, tiles;           // FP64 warp tiles: per row band, and in all
   long long cells;
   // FP32 refinement buffers (filled on the first batched FP32 solve)
   G32 g32;
   IrPtrs q;
   float *p32, *pb32;
-  int ntx32, tiles32;
+  int ntx32, tiles32;       // FP32 warp tiles
 };
 
 struct BatchMap {
@@ -117,11 +121,10 @@ __device__ __forceinline__ void finish_deck(double (&acc)[N], const Op &op, int 
 
 template <class Op>
 __device__ __forceinline__ void walk_deck(const DeckDesc &D, const Op &op, int lb, int nblocks, double (&acc)[1]) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int TW = 64 * BATCH_WARPS;
-  for (int t = lb; t < D.tiles; t += nblocks) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int t = lb * nw + warp; t < D.tiles; t += nblocks * nw) {
     const int tx = t % D.ntx, ty = t / D.ntx;
-    const int i0 = tx * TW + warp * 64 + 2 * lane;
+    const int i0 = tx * 64 + 2 * lane;
     const int j0 = ty * BATCH_ROWS;
     const int j1 = min(j0 + BATCH_ROWS, D.g.ny);
     op.tile(i0, j0, j1, acc);
@@ -169,14 +172,13 @@ __global__ void __launch_bounds__(256) k_batch_ur(const DeckDesc *decks, const B
 
 // ---- FP32 refinement --------------------------------------------------------
 
-// Walk with four cells per lane: tiles of 128*BATCH_WARPS columns x BATCH_ROWS rows.
+// Walk with four cells per lane over the deck's FP32 warp tiles.
 template <class Op>
 __device__ __forceinline__ void walk_deck32(const DeckDesc &D, const Op &op, int lb, int nblocks, double (&acc)[1]) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int TW = 128 * BATCH_WARPS;
-  for (int t = lb; t < D.tiles32; t += nblocks) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int t = lb * nw + warp; t < D.tiles32; t += nblocks * nw) {
     const int tx = t % D.ntx32, ty = t / D.ntx32;
-    const int i0 = tx * TW + warp * 128 + 4 * lane;
+    const int i0 = tx * 128 + 4 * lane;
     const int j0 = ty * BATCH_ROWS;
     const int j1 = min(j0 + BATCH_ROWS, D.g.ny);
     op.tile(i0, j0, j1, acc);
@@ -331,8 +333,8 @@ __global__ void k_batch_ir_start(DevScalars *sc, double delta2) {
 }
 
 // Shares `total` blocks over the unconverged decks in proportion to their
-// cells: one each, the rest in proportion (rounded down), at most one block
-// per tile.
+// cells: one each, the rest in proportion (rounded down), at most as many
+// blocks as the deck's warp tiles can fill.
 __device__ void share(const DeckDesc *decks, BatchMap *map, const int *act, int total, int *first, int *nblk) {
   __shared__ long long cells_sum;
   __shared__ int spare;
@@ -354,7 +356,8 @@ __device__ void share(const DeckDesc *decks, BatchMap *map, const int *act, int 
     if (act[d]) {
       const double want = cells_sum > 0 ? (double)spare * (double)decks[d].cells / (double)cells_sum : 0.0;
       b = 1 + (int)want;
-      if (b > decks[d].tiles) b = decks[d].tiles;
+      const int cap = (decks[d].tiles + BATCH_WARPS - 1) / BATCH_WARPS;  // every block has a warp tile
+      if (b > cap) b = cap;
     }
     nblk[d] = b;
   }
@@ -506,7 +509,7 @@ extern "C" int tl_batch_create(tl_batch **out, tl_ctx *const *ctxs, int n) {
     b->ctx.push_back(c);
     h[k].F = c->F;
     h[k].g = c->g;
-    h[k].ntx = (c->g.nx + 64 * BATCH_WARPS - 1) / (64 * BATCH_WARPS);
+    h[k].ntx = (c->g.nx + 63) / 64;
     h[k].tiles = h[k].ntx * ((c->g.ny + BATCH_ROWS - 1) / BATCH_ROWS);
     h[k].cells = (long long)c->g.nx * c->g.ny;
   }
@@ -604,7 +607,7 @@ int batch_solve_ir(tl_batch *b, const double *rx, const double *ry, const tl_par
       D.q.x = ctx->ir->x;
       D.p32 = ctx->ir->p;
       D.pb32 = ctx->ir->pb;
-      D.ntx32 = (ctx->g.nx + 128 * BATCH_WARPS - 1) / (128 * BATCH_WARPS);
+      D.ntx32 = (ctx->g.nx + 127) / 128;
       D.tiles32 = D.ntx32 * ((ctx->g.ny + BATCH_ROWS - 1) / BATCH_ROWS);
     }
     BCK(cudaMemcpyAsync(b->d_decks, b->h_decks.data(), sizeof(DeckDesc) * n, cudaMemcpyHostToDevice, b->stream));
