@@ -55,6 +55,7 @@ struct BatchMap {
   int total_w, total_u;     // blocks of the W and UR launches
   int first_w[BATCH_MAX + 1], nblk_w[BATCH_MAX];
   int first_u[BATCH_MAX + 1], nblk_u[BATCH_MAX];
+  int first_r[BATCH_MAX + 1], nblk_r[BATCH_MAX];  // FP32 refinement: all blocks over the refining decks
 };
 
 __device__ __forceinline__ int find_deck(const int *first, const int *nblk, int n, int b) {
@@ -241,11 +242,11 @@ __device__ __forceinline__ bool refining(const DeckDesc &D) { return D.F.sc->don
 // Refinement, FP64: u += x, x = 0; the current search direction moves to the
 // first buffer.
 __global__ void k_batch_ir_fold(const DeckDesc *decks, const BatchMap *map) {
-  const int d = find_deck(map->first_w, map->nblk_w, map->n, blockIdx.x);
+  const int d = find_deck(map->first_r, map->nblk_r, map->n, blockIdx.x);
   if (d < 0) return;
   const DeckDesc &D = decks[d];
   if (!refining(D)) return;
-  const int lb = blockIdx.x - map->first_w[d], nb = map->nblk_w[d];
+  const int lb = blockIdx.x - map->first_r[d], nb = map->nblk_r[d];
   const bool move = D.F.sc->pbuf != 0;
   const long long n = (long long)D.g.nx * D.g.ny;
   for (long long k = (long long)lb * blockDim.x + threadIdx.x; k < n; k += (long long)nb * blockDim.x) {
@@ -259,11 +260,11 @@ __global__ void k_batch_ir_fold(const DeckDesc *decks, const BatchMap *map) {
 
 // Refinement: the reflective halo of u, depth 1, faces only (corners untouched).
 __global__ void k_batch_ir_halo(const DeckDesc *decks, const BatchMap *map) {
-  const int d = find_deck(map->first_w, map->nblk_w, map->n, blockIdx.x);
+  const int d = find_deck(map->first_r, map->nblk_r, map->n, blockIdx.x);
   if (d < 0) return;
   const DeckDesc &D = decks[d];
   if (!refining(D)) return;
-  const int lb = blockIdx.x - map->first_w[d], nb = map->nblk_w[d];
+  const int lb = blockIdx.x - map->first_r[d], nb = map->nblk_r[d];
   const int nx = D.g.nx, ny = D.g.ny;
   double *u = D.F.u;
   for (int k = lb * blockDim.x + threadIdx.x; k < 2 * (nx + ny); k += nb * blockDim.x) {
@@ -299,7 +300,7 @@ struct OpIrResidBatch : OpIrResid {
 };
 
 __global__ void __launch_bounds__(256) k_batch_ir_resid(const DeckDesc *decks, const BatchMap *map) {
-  const int d = find_deck(map->first_w, map->nblk_w, map->n, blockIdx.x);
+  const int d = find_deck(map->first_r, map->nblk_r, map->n, blockIdx.x);
   if (d < 0) return;
   const DeckDesc &D = decks[d];
   if (!refining(D)) return;
@@ -309,7 +310,7 @@ __global__ void __launch_bounds__(256) k_batch_ir_resid(const DeckDesc *decks, c
   op.g32 = D.g32;
   op.r32 = D.q.r;
   double acc[1] = {0.0};
-  const int lb = blockIdx.x - map->first_w[d], nb = map->nblk_w[d];
+  const int lb = blockIdx.x - map->first_r[d], nb = map->nblk_r[d];
   walk_deck(D, op, lb, nb, acc);
   finish_deck<1>(acc, op, nb, lb);
 }
@@ -371,6 +372,16 @@ __device__ void share(const DeckDesc *decks, BatchMap *map, const int *act, int 
     first[n] = f;
   }
   __syncthreads();
+}
+
+// Shares the blocks of the refinement kernels over the decks whose inner loop
+// has just ended, so that a refinement runs on the whole GPU and not on one
+// deck's share of it.
+__global__ void k_batch_refine_map(const DeckDesc *decks, BatchMap *map) {
+  __shared__ int act[BATCH_MAX];
+  for (int d = threadIdx.x; d < map->n; d += blockDim.x) act[d] = refining(decks[d]) ? 1 : 0;
+  __syncthreads();
+  share(decks, map, act, map->total_w, map->first_r, map->nblk_r);
 }
 
 // Rebuilds the block map over the decks still running and sets the loop
@@ -466,6 +477,7 @@ int build_graph(tl_batch *b, int ir) {
     }
   }
   if (ir) {
+    k_batch_refine_map<<<1, 256, 0, b->stream>>>(b->d_decks, b->d_map);
     k_batch_ir_fold<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map);
     k_batch_ir_halo<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map);
     k_batch_ir_resid<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map);
