@@ -19,7 +19,6 @@ namespace {
 
 using bf16 = __nv_bfloat16;
 constexpr int TP = 64;  // pixels of one image row per block (4 warps x 16)
-constexpr int RB = 8;   // image rows swept by one forward block
 
 __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
   asm volatile(
@@ -60,10 +59,38 @@ struct ConvArgs {
   int N, H, W;
 };
 
-// One block: TP pixels x RB rows of one image, all COUT channels; warp w owns
-// pixels [16w, 16w+16) of the row being computed.  The weights stay in shared
-// memory for the whole sweep; the three input rows live in a ring and one new
-// row is loaded per output row.  K = 9 taps x CIN in steps of 16.
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void *p) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(s));
+}
+
+// 16-byte asynchronous copy global -> shared; `bytes` = 0 writes zeros
+// (the source address must still be a valid one).
+__device__ __forceinline__ void cp_async16(void *dst, const void *src, int bytes) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(src), "r"(bytes));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
+
+constexpr int FTP = 128;  // forward: pixels of one image row per block (4 warps x 32)
+constexpr int FRB = 16;   // forward: image rows swept by one block
+
+template <int CIN, int COUT>
+constexpr int conv_smem_bytes() {
+  return 2 * (COUT * (9 * CIN + 8) + 4 * (FTP + 2) * (CIN + 8));
+}
+
+// One block: FTP pixels x FRB rows of one image, all COUT channels; warp w
+// owns pixels [32w, 32w+32) (two 16-pixel m-tiles) of the row being
+// computed.  The weights stay in shared memory for the whole sweep.  Input
+// rows live in a four-slot ring filled by cp.async: row y+2 is fetched while
+// row y is computed, and one barrier per row both publishes the new row and
+// frees the slot the next fetch overwrites.  K = 9 taps x CIN in steps of 16;
+// A (pixels x channels) and B (channels x output channels) fragments come
+// from ldmatrix.
 // MODE 0: out = z; 1: out = GELU(z) (z stored when `z` is set);
 // 2: out = z * GELU'(gz) (input gradient fused with the GELU derivative).
 // `out32` (when set) receives channel 0 of z in FP32.
@@ -73,93 +100,107 @@ __global__ void __launch_bounds__(128) k_conv3x3(ConvArgs a) {
   constexpr int WS = 9 * CIN + 8;  // weight row stride
   constexpr int NT = COUT / 8;
   constexpr int V = CIN / 8;       // 16-byte vectors per pixel
-  __shared__ __align__(16) bf16 sw[COUT][WS];
-  __shared__ __align__(16) bf16 sx[3][TP + 2][PS];
-  const int img = blockIdx.z, x0 = blockIdx.x * TP, y0 = blockIdx.y * RB;
-  const int y1 = min(a.H, y0 + RB);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  bf16 *sw = reinterpret_cast<bf16 *>(smem_raw);                   // [COUT][WS]
+  bf16 *sx = sw + COUT * WS;                                        // [4][FTP + 2][PS]
+  const int img = blockIdx.z, x0 = blockIdx.x * FTP, y0 = blockIdx.y * FRB;
+  const int y1 = min(a.H, y0 + FRB);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int g = lane >> 2, t = lane & 3, px = warp * 16;
+  const int g = lane >> 2, t = lane & 3, px = warp * 32;
   const size_t plane = (size_t)a.H * a.W;
   const bf16 *xi = a.x + (size_t)img * plane * CIN;
 
   for (int v = tid; v < COUT * 9 * V; v += 128) {
     const int row = v / (9 * V), c = v % (9 * V);
-    *reinterpret_cast<uint4 *>(&sw[row][c * 8]) = reinterpret_cast<const uint4 *>(a.w)[v];
+    cp_async16(sw + row * WS + c * 8, a.w + (size_t)v * 8, 16);
   }
   auto load_row = [&](int yy) {
-    const int slot = (yy + 3) % 3;
-    for (int v = tid; v < (TP + 2) * V; v += 128) {
+    bf16 *dst = sx + ((yy + 4) & 3) * (FTP + 2) * PS;
+    for (int v = tid; v < (FTP + 2) * V; v += 128) {
       const int col = v / V, c8 = v % V, xx = x0 + col - 1;
-      uint4 val = make_uint4(0, 0, 0, 0);
-      if (yy >= 0 && yy < a.H && xx >= 0 && xx < a.W)
-        val = *reinterpret_cast<const uint4 *>(xi + ((size_t)yy * a.W + xx) * CIN + c8 * 8);
-      *reinterpret_cast<uint4 *>(&sx[slot][col][c8 * 8]) = val;
+      const bool in = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
+      const bf16 *src = in ? xi + ((size_t)yy * a.W + xx) * CIN + c8 * 8 : xi;
+      cp_async16(dst + col * PS + c8 * 8, src, in ? 16 : 0);
     }
   };
   load_row(y0 - 1);
   load_row(y0);
+  load_row(y0 + 1);
+  cp_async_commit();
+  cp_async_wait_all();
+  __syncthreads();
+  // ldmatrix row addresses: A matrix j = lane/8 covers pixels +8*(j&1), channels +8*(j>>1);
+  // B matrix j covers output channels +8*(j>>1), k +8*(j&1)
+  const int lj = lane >> 3, lr = lane & 7;
   for (int y = y0; y < y1; ++y) {
-    __syncthreads();  // the previous row's reads of the slot being replaced are done
-    load_row(y + 1);
-    __syncthreads();
-    float acc[NT][4];
+    if (y + 2 <= y1) {
+      load_row(y + 2);
+      cp_async_commit();
+    }
+    float acc[2][NT][4];
 #pragma unroll
-    for (int n = 0; n < NT; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+      for (int n = 0; n < NT; ++n) acc[m][n][0] = acc[m][n][1] = acc[m][n][2] = acc[m][n][3] = 0.f;
 #pragma unroll
     for (int dy = 0; dy < 3; ++dy) {
-      const int slot = (y - 1 + dy + 3) % 3;
+      const bf16 *srow = sx + ((y - 1 + dy + 4) & 3) * (FTP + 2) * PS;
 #pragma unroll
       for (int dx = 0; dx < 3; ++dx) {
         const int tap = 3 * dy + dx;
 #pragma unroll
         for (int cc = 0; cc < CIN; cc += 16) {
-          const bf16 *r0 = &sx[slot][px + g + dx][cc];
-          const bf16 *r8 = &sx[slot][px + g + 8 + dx][cc];
-          uint32_t af[4];
-          af[0] = *reinterpret_cast<const uint32_t *>(r0 + 2 * t);
-          af[1] = *reinterpret_cast<const uint32_t *>(r8 + 2 * t);
-          af[2] = *reinterpret_cast<const uint32_t *>(r0 + 2 * t + 8);
-          af[3] = *reinterpret_cast<const uint32_t *>(r8 + 2 * t + 8);
+          uint32_t af[2][4];
 #pragma unroll
-          for (int n = 0; n < NT; ++n) {
-            const bf16 *wc = &sw[n * 8 + g][tap * CIN + cc];
-            uint32_t bfr[2];
-            bfr[0] = *reinterpret_cast<const uint32_t *>(wc + 2 * t);
-            bfr[1] = *reinterpret_cast<const uint32_t *>(wc + 2 * t + 8);
-            mma_bf16(acc[n], af, bfr);
+          for (int m = 0; m < 2; ++m)
+            ldsm_x4(af[m], srow + (px + 16 * m + 8 * (lj & 1) + lr + dx) * PS + cc + 8 * (lj >> 1));
+#pragma unroll
+          for (int n2 = 0; n2 < NT; n2 += 2) {
+            uint32_t bq[4];
+            ldsm_x4(bq, sw + (n2 * 8 + 8 * (lj >> 1) + lr) * WS + tap * CIN + cc + 8 * (lj & 1));
+            const uint32_t b0[2] = {bq[0], bq[1]}, b1[2] = {bq[2], bq[3]};
+#pragma unroll
+            for (int m = 0; m < 2; ++m) {
+              mma_bf16(acc[m][n2], af[m], b0);
+              mma_bf16(acc[m][n2 + 1], af[m], b1);
+            }
           }
         }
       }
     }
-    // rows g and g+8 of the warp's 16 pixels; channels n*8 + 2t, +1
+    // rows g and g+8 of each 16-pixel m-tile; channels n*8 + 2t, +1
 #pragma unroll
-    for (int half = 0; half < 2; ++half) {
-      const int xx = x0 + px + g + 8 * half;
-      if (xx >= a.W) continue;
-      const size_t pix = (size_t)img * plane + (size_t)y * a.W + xx;
-      const size_t o = pix * COUT;
+    for (int m = 0; m < 2; ++m)
 #pragma unroll
-      for (int n = 0; n < NT; ++n) {
-        const int ch = n * 8 + 2 * t;
-        float z0 = acc[n][2 * half], z1 = acc[n][2 * half + 1];
-        if (a.bias) {
-          z0 += a.bias[ch];
-          z1 += a.bias[ch + 1];
+      for (int half = 0; half < 2; ++half) {
+        const int xx = x0 + px + 16 * m + g + 8 * half;
+        if (xx >= a.W) continue;
+        const size_t pix = (size_t)img * plane + (size_t)y * a.W + xx;
+        const size_t o = pix * COUT;
+#pragma unroll
+        for (int n = 0; n < NT; ++n) {
+          const int ch = n * 8 + 2 * t;
+          float z0 = acc[m][n][2 * half], z1 = acc[m][n][2 * half + 1];
+          if (a.bias) {
+            z0 += a.bias[ch];
+            z1 += a.bias[ch + 1];
+          }
+          if (a.out32 && ch == 0) a.out32[pix] = z0;
+          float o0 = z0, o1 = z1;
+          if (MODE == 1) {
+            if (a.z) *reinterpret_cast<__nv_bfloat162 *>(a.z + o + ch) = __floats2bfloat162_rn(z0, z1);
+            o0 = gelu(z0);
+            o1 = gelu(z1);
+          } else if (MODE == 2) {
+            const __nv_bfloat162 zz = *reinterpret_cast<const __nv_bfloat162 *>(a.gz + o + ch);
+            o0 = z0 * gelu_grad(__low2float(zz));
+            o1 = z1 * gelu_grad(__high2float(zz));
+          }
+          if (a.out) *reinterpret_cast<__nv_bfloat162 *>(a.out + o + ch) = __floats2bfloat162_rn(o0, o1);
         }
-        if (a.out32 && ch == 0) a.out32[pix] = z0;
-        float o0 = z0, o1 = z1;
-        if (MODE == 1) {
-          if (a.z) *reinterpret_cast<__nv_bfloat162 *>(a.z + o + ch) = __floats2bfloat162_rn(z0, z1);
-          o0 = gelu(z0);
-          o1 = gelu(z1);
-        } else if (MODE == 2) {
-          const __nv_bfloat162 zz = *reinterpret_cast<const __nv_bfloat162 *>(a.gz + o + ch);
-          o0 = z0 * gelu_grad(__low2float(zz));
-          o1 = z1 * gelu_grad(__high2float(zz));
-        }
-        if (a.out) *reinterpret_cast<__nv_bfloat162 *>(a.out + o + ch) = __floats2bfloat162_rn(o0, o1);
       }
-    }
+    cp_async_wait_all();
+    __syncthreads();
   }
 }
 
@@ -423,12 +464,23 @@ inline int grid_for(long long n) {
   return (int)(b < 1 ? 1 : b);
 }
 
+template <int CIN, int COUT, int MODE>
+void launch_conv_mode(const ConvArgs &a, cudaStream_t st) {
+  constexpr int smem = conv_smem_bytes<CIN, COUT>();
+  static bool attr = false;  // the dynamic shared memory limit, set once per kernel
+  if (!attr) {
+    cudaFuncSetAttribute(k_conv3x3<CIN, COUT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    attr = true;
+  }
+  const dim3 grid((a.W + FTP - 1) / FTP, (a.H + FRB - 1) / FRB, a.N);
+  k_conv3x3<CIN, COUT, MODE><<<grid, 128, smem, st>>>(a);
+}
+
 template <int CIN, int COUT>
 void launch_conv(const ConvArgs &a, int mode, cudaStream_t st) {
-  const dim3 grid((a.W + TP - 1) / TP, (a.H + RB - 1) / RB, a.N);
-  if (mode == 0) k_conv3x3<CIN, COUT, 0><<<grid, 128, 0, st>>>(a);
-  else if (mode == 1) k_conv3x3<CIN, COUT, 1><<<grid, 128, 0, st>>>(a);
-  else k_conv3x3<CIN, COUT, 2><<<grid, 128, 0, st>>>(a);
+  if (mode == 0) launch_conv_mode<CIN, COUT, 0>(a, st);
+  else if (mode == 1) launch_conv_mode<CIN, COUT, 1>(a, st);
+  else launch_conv_mode<CIN, COUT, 2>(a, st);
 }
 
 }  // namespace
@@ -437,7 +489,7 @@ int tl_conv_forward(const void *x, const void *w, const float *bias, const void 
                     int N, int H, int W, int cin, int cout, int mode, cudaStream_t st) {
   if (!x || !w || (!out && !out32) || N < 1 || H < 1 || W < 1 || mode < 0 || mode > 2) return TL_ERR_ARG;
   if (mode == 2 && !gz) return TL_ERR_ARG;
-  if (N > 65535 || (H + RB - 1) / RB > 65535) return TL_ERR_ARG;
+  if (N > 65535 || (H + FRB - 1) / FRB > 65535) return TL_ERR_ARG;
   ConvArgs a;
   a.x = static_cast<const bf16 *>(x);
   a.w = static_cast<const bf16 *>(w);

@@ -229,3 +229,36 @@ def test_trained_network_gain_is_measured_and_bounded(tl, built_lib):
         assert ev[k]["final_rel_diff"] < 1e-8
     assert tot["network"] <= 1.15 * tot["plain"]
     assert tot["extrapolate"] <= tot["plain"]
+
+
+@pytest.mark.parametrize("cin,cout,mode", [(16, 32, 1), (32, 32, 1), (32, 16, 0), (32, 32, 2), (16, 32, 0)])
+def test_conv_forward_ragged_shapes(tl, built_lib, cin, cout, mode):
+    """The forward kernel on images whose width spans two 128-pixel segments
+    with a ragged end and whose height is not a multiple of the 16-row sweep,
+    two images, every mode: against the oracle's convolution."""
+    N, H, Wd = 2, 37, 150
+    rng = np.random.default_rng(cin * 7 + cout + mode)
+    x = W.bf16(rng.standard_normal((N, H, Wd, cin)))
+    w = W.bf16(0.1 * rng.standard_normal((cout, 9, cin)))
+    b = rng.standard_normal(cout).astype(np.float32).astype(np.float64)
+    gz = W.bf16(rng.standard_normal((N, H, Wd, cout)))
+    dev = lambda a: torch.tensor(a, dtype=torch.float32, device="cuda").to(torch.bfloat16)  # noqa: E731
+    xd, wd, gzd = dev(x), dev(w.reshape(-1)), dev(gz)
+    bd = torch.tensor(b, dtype=torch.float32, device="cuda")
+    out = torch.zeros((N, H, Wd, cout), dtype=torch.bfloat16, device="cuda")
+    zd = torch.zeros_like(out)
+    g32 = torch.zeros((N, H, Wd), dtype=torch.float32, device="cuda")
+    lib = tl._abi.load()
+    st = torch.cuda.current_stream().cuda_stream
+    rc = lib.tl_conv3x3_forward(xd.data_ptr(), wd.data_ptr(), bd.data_ptr() if mode != 2 else None,
+                                gzd.data_ptr() if mode == 2 else None, zd.data_ptr() if mode == 1 else None,
+                                out.data_ptr(), g32.data_ptr(), N, H, Wd, cin, cout, mode, st)
+    assert rc == 0
+    torch.cuda.synchronize()
+    z = W.conv(x, w) + (b if mode != 2 else 0.0)
+    ref = {0: z, 1: W.gelu(z), 2: z * W.gelu_grad(gz)}[mode]
+    close_bf16(f64(out), W.bf16(ref), f"conv {cin}->{cout} mode {mode}")
+    if mode == 1:
+        close_bf16(f64(zd), W.bf16(z), "pre-activation")
+    gg = g32.cpu().numpy().astype(np.float64)
+    assert np.max(np.abs(gg - z[..., 0])) <= 1e-5 * np.max(np.abs(z[..., 0]))
