@@ -142,6 +142,21 @@ __global__ void __launch_bounds__(128) k_conv3x3(ConvArgs a) {
     for (int m = 0; m < 2; ++m)
 #pragma unroll
       for (int n = 0; n < NT; ++n) acc[m][n][0] = acc[m][n][1] = acc[m][n][2] = acc[m][n][3] = 0.f;
+    // MODE 2: the epilogue's GELU' inputs, loaded before the MMAs so that
+    // their latency overlaps the math
+    __nv_bfloat162 gzr[2][2][MODE == 2 ? NT : 1];
+    if (MODE == 2) {
+#pragma unroll
+      for (int m = 0; m < 2; ++m)
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+          const int xx = x0 + px + 16 * m + g + 8 * half;
+          const size_t o = ((size_t)img * plane + (size_t)y * a.W + (xx < a.W ? xx : 0)) * COUT;
+#pragma unroll
+          for (int n = 0; n < (MODE == 2 ? NT : 1); ++n)
+            gzr[m][half][n] = *reinterpret_cast<const __nv_bfloat162 *>(a.gz + o + n * 8 + 2 * t);
+        }
+    }
 #pragma unroll
     for (int dy = 0; dy < 3; ++dy) {
       const bf16 *srow = sx + ((y - 1 + dy + 4) & 3) * (FTP + 2) * PS;
@@ -192,7 +207,7 @@ __global__ void __launch_bounds__(128) k_conv3x3(ConvArgs a) {
             o0 = gelu(z0);
             o1 = gelu(z1);
           } else if (MODE == 2) {
-            const __nv_bfloat162 zz = *reinterpret_cast<const __nv_bfloat162 *>(a.gz + o + ch);
+            const __nv_bfloat162 zz = gzr[m][half][MODE == 2 ? n : 0];
             o0 = z0 * gelu_grad(__low2float(zz));
             o1 = z1 * gelu_grad(__high2float(zz));
           }
