@@ -246,8 +246,8 @@ int tl_field_summary_noalloc(const double *volume, const double *density, const 
  * the true residual.  A smaller initial residual does not imply fewer
  * iterations, so runs of at most `trust` (2, 4, ... 32) solves from the
  * prediction are bracketed by control solves from the plain start; a run that
- * needed more iterations than its controls, or a prediction the residual test
- * rejected, pauses the prediction for 4, 8, ... 64 steps.
+ * needed more iterations than its controls, or a network prediction the
+ * residual test rejected, pauses the prediction for 4, 8, ... 64 steps.
  *
  * Parameter vector (FP32, TL_WARM_NPARAMS values), layer by layer:
  * W[cout][9][cin] then b[cout], with (cin, cout) = (16, 32), (32, 32) x 4,

@@ -378,7 +378,7 @@ int tl_cg_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_resu
   res->converged = ran && (prm->criterion == TL_CRIT_RELATIVE ? (rel >= 0 && rel < prm->eps) : sc.converged);
   res->rel_residual = rel;
   res->launches = (int)ctx->launches;
-  if (prm->warmstart) tl_warm_after(ctx, res);
+  if (prm->warmstart) tl_warm_after(ctx, res, prm->warmstart);
   return TL_OK;
 }
 

@@ -90,7 +90,7 @@ tl::Walk *tl_ir_walk(tl_ctx *ctx, int kernel);  // the FP32 kernels' layouts (ke
 // plain start by the network's prediction; always records u^n for the next step.
 int tl_warm_try(tl_ctx *ctx, double rx, double ry, int warmstart, tl_result *res);
 // after the solve: the iteration guard
-void tl_warm_after(tl_ctx *ctx, const tl_result *res);
+void tl_warm_after(tl_ctx *ctx, const tl_result *res, int warmstart);
 void tl_release_warm(tl_ctx *ctx);
 
 #define CK(x)                                                     \

@@ -353,10 +353,10 @@ int tl_warm_try(tl_ctx *ctx, double rx, double ry, int warmstart, tl_result *res
 // from the plain start.  When a run's mean iteration count exceeds the mean of
 // its two controls, the prediction pauses for `backoff` steps (4, 8, ... 64)
 // and trust drops to 2; otherwise trust doubles (up to 32) and the backoff
-// returns to 4.  A prediction rejected by the residual judge (outside a run)
-// pauses the next ones the same way, so that rejected inference stops
-// costing time.
-void tl_warm_after(tl_ctx *ctx, const tl_result *res) {
+// returns to 4.  A network prediction rejected by the residual judge
+// (outside a run) pauses the next ones the same way, so that rejected
+// inference stops costing time.
+void tl_warm_after(tl_ctx *ctx, const tl_result *res, int warmstart) {
   tl_warm_state *ws = ctx->warm;
   if (!ws) return;
   if (res->warm == 1) {
@@ -364,9 +364,10 @@ void tl_warm_after(tl_ctx *ctx, const tl_result *res) {
     ws->run_iters += res->iters;
     return;
   }
-  if (res->warm == 2 && ws->run == 0) {
-    // the prediction lost to the plain start by residual: its inference was
-    // wasted, so the next attempts back off the same way
+  if (res->warm == 2 && ws->run == 0 && warmstart == TL_WARM_NETWORK) {
+    // the network's prediction lost to the plain start by residual: its
+    // inference was wasted, so the next attempts back off the same way (the
+    // extrapolation candidate costs one pass and is tried every step)
     ws->cooloff = ws->backoff;
     ws->backoff = ws->backoff < 64 ? 2 * ws->backoff : 64;
   }

@@ -199,7 +199,7 @@ def test_warm_start_judge_and_accuracy(tl, built_lib, precision):
             if used == 1:
                 run, run_iters = run + 1, run_iters + it
                 continue
-            if used == 2 and run == 0:
+            if used == 2 and run == 0 and name == "network":
                 cooloff, backoff = backoff, min(2 * backoff, 64)
             if run:
                 if run_iters / run > 0.5 * (ctrl + it):
