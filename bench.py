@@ -452,6 +452,24 @@ def run_config2(args):
         chunk.close()
         out["solvers"][solver] = {"runs": runs, "ms_per_run": statistics.mean(r["ms"] for r in runs),
                                   "kernels_after_solve": kern}
+    # the same decks to the relative true residual 1e-10: FP64 and FP32 inside
+    # FP64 refinement, CG and Chebyshev (one run each)
+    out["relative"] = {}
+    for solver in ("cg", "cheby"):
+        for prec, pname in ((0, "fp64"), (1, "fp32_refined")):
+            s = tl.Settings.from_text(config2_deck(n, solver), mode=1, exact=False, criterion=1, precision=prec)
+            chunk = tl.initialiseapp(s)
+            lib = chunk.lib
+            chunk.check(lib.tl_synchronize(chunk.ctx))
+            chunk.check(lib.tl_timer_start(chunk.ctx))
+            steps, sums = tl.diffuse(chunk, s, problemfile=None)
+            ms = C.c_double()
+            chunk.check(lib.tl_timer_stop(chunk.ctx, C.byref(ms)))
+            out["relative"][f"{solver}_{pname}"] = {
+                "ms": ms.value, "iters": [r.iters for r in steps], "inner_iters": [r.inner_iters for r in steps],
+                "refinements": [r.refinements for r in steps], "rel_residual_max": max(r.rel_residual for r in steps),
+                "converged": all(r.converged for r in steps), "summary": sums[-1]}
+            chunk.close()
     out["peak_gbs"] = peak
     out["peak_kind"] = peak_kind
     if not args.no_cpu:

@@ -165,10 +165,13 @@ void tl_release_ir(tl_ctx *ctx) {
   ctx->ir = nullptr;
 }
 
-// The refinement step.  Returns the true r.r in *rr.
-static int refine(tl_ctx *ctx, double *rr) {
+// The refinement step: u += e, e = 0 (e: the FP32 correction, x by
+// default), the halo of u, the true residual r = u0 - A u in FP64 and its
+// FP32 copy.  Returns the true r.r in *rr.
+static int refine(tl_ctx *ctx, double *rr, float *e = nullptr) {
   const G32 g32 = g32_of(ctx);
-  k_ir_fold<<<grid_for((long long)ctx->g.nx * ctx->g.ny), 256, 0, ctx->stream>>>(ctx->F, ctx->g, g32, ctx->ir->x);
+  k_ir_fold<<<grid_for((long long)ctx->g.nx * ctx->g.ny), 256, 0, ctx->stream>>>(ctx->F, ctx->g, g32,
+                                                                                e ? e : ctx->ir->x);
   CKL();
   double *u = ctx->F.u;
   launch_halo(ctx->stream, &u, 1, ctx->g, 1, TL_MODE_TEALEAF);
@@ -290,4 +293,206 @@ int tl_ir_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch)
 tl::Walk *tl_ir_walk(tl_ctx *ctx, int kernel) {
   if (ensure_ir(ctx)) return nullptr;
   return kernel == 2 ? &ctx->ir->walk_w : &ctx->ir->walk_ur;
+}
+
+// ---------------------------------------------------------------------------
+// Chebyshev steps in FP32 inside FP64 refinement
+// ---------------------------------------------------------------------------
+
+namespace tl {
+namespace {
+
+// One FP32 Chebyshev step on the correction e of the current refinement
+// (A e = r0): w = A e (difference form, reflective boundary in the index
+// math), r = r0 - w, p = alpha_k p + beta_k r, e' = e + p, and r.r (each
+// lane's four products summed in FP32, accumulated in FP64).  The epilogue
+// counts the step and asks for a refinement once r.r has dropped by delta^2
+// or claims convergence.
+struct OpCheby32 {
+  static constexpr bool REDUCES = true;
+  Fields F;
+  G32 g;
+  IrPtrs q;  // kx, ky, r (= r0)
+  const float *__restrict__ esrc;
+  float *__restrict__ edst;
+  float *__restrict__ p;
+  int guard;
+  __device__ bool skip() const { return guard && F.sc->done; }
+  __device__ void on_skip() const {}
+
+  __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
+    const int nx = g.nx, ny = g.ny;
+    const int lane = threadIdx.x & 31;
+    const bool valid = i0 < nx;
+    const int ncell = valid ? min(4, nx - i0) : 0;
+    const bool full = ncell == 4;
+    const bool inner = i0 + 4 < nx;
+    const int k = F.sc->cheby_iters + 1;
+    const int idx = min(k + 1, F.sc->maxiters + 1);
+    const float ca = (float)F.chebyalpha[idx], cb = (float)F.chebybeta[idx];
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto ld = [&](const float *a, int j) { return valid ? ld4(a + g.at(i0, j)) : z; };
+    float4 ec = ld(esrc, j0);
+    float4 es = j0 > 0 ? ld(esrc, j0 - 1) : ec;
+    float4 kys = ld(q.ky, j0);
+    float a = 0.f;
+    for (int j = j0; j < j1; ++j) {
+      const float4 en = j + 1 < ny ? ld(esrc, j + 1) : ec;
+      const float4 kyn = ld(q.ky, j + 1);
+      const float4 kx = ld(q.kx, j);
+      const float4 r0 = ld(q.r, j);
+      const float4 pv = ld(p, j);
+      float ew = __shfl_up_sync(FULL, ec.w, 1);
+      float ee = __shfl_down_sync(FULL, ec.x, 1);
+      float kxe = __shfl_down_sync(FULL, kx.x, 1);
+      if (valid) {
+        if (i0 == 0) ew = ec.x;
+        else if (lane == 0) ew = __ldg(esrc + g.at(i0 - 1, j));
+        if (full && (lane == 31 || !inner)) {
+          kxe = __ldg(q.kx + g.at(i0 + 4, j));
+          ee = inner ? __ldg(esrc + g.at(i0 + 4, j)) : ec.w;
+        }
+        float pn[4], en4[4];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          pn[m] = 0.f;
+          en4[m] = 0.f;
+          if (m < ncell) {
+            const float c = comp(ec, m);
+            const float e = (m + 1 < ncell) ? comp(ec, m + 1) : (m == 3 ? ee : c);
+            const float wl = (m == 0) ? ew : comp(ec, m - 1);
+            const float k1 = (m == 3) ? kxe : comp(kx, m + 1);
+            float w = c;
+            w = fmaf(k1, c - e, w);
+            w = fmaf(comp(kx, m), c - wl, w);
+            w = fmaf(comp(kyn, m), c - comp(en, m), w);
+            w = fmaf(comp(kys, m), c - comp(es, m), w);
+            const float r = comp(r0, m) - w;
+            pn[m] = fmaf(ca, comp(pv, m), cb * r);
+            en4[m] = c + pn[m];
+            a = fmaf(r, r, a);
+          }
+        }
+        const size_t c0 = g.at(i0, j);
+        if (full) {
+          st4(p + c0, make_float4(pn[0], pn[1], pn[2], pn[3]));
+          st4(edst + c0, make_float4(en4[0], en4[1], en4[2], en4[3]));
+        } else {
+          for (int m = 0; m < ncell; ++m) {
+            p[c0 + m] = pn[m];
+            edst[c0 + m] = en4[m];
+          }
+        }
+      }
+      acc[0] += (double)a;
+      a = 0.f;
+      es = ec;
+      ec = en;
+      kys = kyn;
+    }
+  }
+  __device__ void fin(const double *tot) const {
+    DevScalars *sc = F.sc;
+    const double rr = tot[0];
+    sc->cheby_iters += 1;
+    sc->iter += 1;
+    sc->error = rr;
+    const bool claim = sqrt(rr / sc->bb) < sc->eps;
+    const bool refine = claim || rr < sc->delta2 * sc->rr_ref;
+    sc->converged = 0;
+    sc->switched = refine;
+    sc->done = refine || sc->iter >= sc->maxiters;
+  }
+};
+
+// FP32 copies for the Chebyshev phase: kx, ky (whole arrays), p (interior);
+// both correction buffers zeroed.
+__global__ void k_cheby32_convert(Fields F, Geom g, G32 g32, float *kx, float *ky, float *p, float *e0, float *e1) {
+  const long long n = (long long)g.X * g.Y;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const int I = (int)(k % g.X), J = (int)(k / g.X);
+    const size_t c = (size_t)I + (size_t)J * g.pitch, c32 = (size_t)I + (size_t)J * g32.pitch;
+    kx[c32] = (float)F.kx[c];
+    ky[c32] = (float)F.ky[c];
+    const bool interior = I >= g.hd && I < g.X - g.hd && J >= g.hd && J < g.Y - g.hd;
+    p[c32] = interior ? (float)F.p[c] : 0.f;
+    e0[c32] = 0.f;
+    e1[c32] = 0.f;
+  }
+}
+
+void launch_cheby32(tl_ctx *ctx, const float *esrc, float *edst, int guard) {
+  OpCheby32 op;
+  op.F = ctx->F;
+  op.g = g32_of(ctx);
+  op.q = ptrs_of(ctx);
+  op.esrc = esrc;
+  op.edst = edst;
+  op.p = ctx->ir->p;
+  op.guard = guard;
+  const Walk &wk = ctx->ir->walk_w;
+  k_walk32<OpCheby32><<<wk.blocks, 32 * wk.warps, 0, ctx->stream>>>(op, wk, ctx->g.ny);
+}
+
+}  // namespace
+}  // namespace tl
+
+// The Chebyshev iteration after its switch, in FP32 inside FP64 refinement
+// (tealeaf mode).  On entry the FP64 Chebyshev phase has run its first step
+// (the iterate is in ub after an odd count).  The FP32 steps solve for the
+// correction of the current refinement with the same coefficient sequence;
+// each refinement folds the correction into u, measures the true residual in
+// FP64 and restarts the correction from it, so the recurrence continues
+// unchanged.  Stops on the relative true residual ||u0 - A u|| / ||u0|| < eps
+// or the iteration budget.
+int tl_cheby32_run(tl_ctx *ctx, const tl_params *prm, int *refinements, double *rel_out) {
+  int rc = ensure_ir(ctx);
+  if (rc) return rc;
+  tl_ir_state *ir = ctx->ir;
+  const G32 g32 = g32_of(ctx);
+  if ((rc = tl_read_scalars(ctx))) return rc;
+  if (ctx->host_sc->cheby_iters & 1) {
+    launch_copy_interior(ctx->stream, ctx->F.u, ctx->F.ub, ctx->g);
+    CKL();
+  }
+  k_cheby32_convert<<<grid_for((long long)ctx->g.X * ctx->g.Y), 256, 0, ctx->stream>>>(ctx->F, ctx->g, g32, ir->kx,
+                                                                                       ir->ky, ir->p, ir->x, ir->pb);
+  CKL();
+  double rr;
+  if ((rc = refine(ctx, &rr))) return rc;  // x = 0: the halo of u and the true residual
+  const double bb = ctx->host_sc->bb;
+  double rel = bb > 0 ? sqrt(rr / bb) : sqrt(rr);
+  int nref = 0;
+  float *ea = ir->x, *eb = ir->pb;  // the correction starts each inner loop in ea, zeroed
+  ctx->last_solve_ms = 0.0;
+  while (rel >= prm->eps && ctx->host_sc->iter < prm->maxiters) {
+    k_ir_start<<<1, 1, 0, ctx->stream>>>(ctx->F.sc, rr, IR_DELTA * IR_DELTA);
+    CKL();
+    const int it0 = ctx->host_sc->cheby_iters;
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    for (;;) {
+      for (int s = 0; s < 16; ++s) launch_cheby32(ctx, (s & 1) ? eb : ea, (s & 1) ? ea : eb, 1);
+      CKL();
+      if ((rc = tl_read_scalars(ctx))) return rc;
+      if (ctx->host_sc->done) break;
+    }
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    CK(cudaEventSynchronize(ctx->ev1));
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1));
+    ctx->last_solve_ms += t;
+    const int steps = ctx->host_sc->cheby_iters - it0;
+    ctx->launches += 1 + steps;
+    float *ecur = (steps & 1) ? eb : ea;
+    if ((rc = refine(ctx, &rr, ecur))) return rc;
+    ++nref;
+    rel = bb > 0 ? sqrt(rr / bb) : sqrt(rr);
+    eb = ecur == ir->x ? ir->pb : ir->x;
+    ea = ecur;
+  }
+  k_ir_export_p<<<grid_for((long long)ctx->g.nx * ctx->g.ny), 256, 0, ctx->stream>>>(ctx->F, ctx->g, g32, ir->p);
+  CKL();
+  *refinements = nref;
+  *rel_out = rel;
+  return TL_OK;
 }

@@ -306,6 +306,24 @@ int tl_cheby_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_r
   const int est = calciter(emin, emax, ctx->host_sc->error, ctx->host_sc->bb);
   k_set_est<<<1, 1, 0, ctx->stream>>>(ctx->F.sc, est);
   CKL();
+  if (!ctx->host_sc->done && prm->precision == TL_PREC_FP32_IR && !exact) {
+    // the rest of the iteration in FP32 inside FP64 refinement
+    int nref = 0;
+    double rel = -1.0;
+    if ((rc = tl_cheby32_run(ctx, prm, &nref, &rel))) return rc;
+    const int ex = TL_EX_U;
+    if ((rc = tl_halo_update(ctx, 1, &ex, 1, 1))) return rc;
+    if ((rc = tl_read_scalars(ctx))) return rc;
+    fill_result(ctx, res, cgiters);
+    res->inner_iters = ctx->host_sc->cheby_iters;
+    res->est_iters = est;
+    res->eigmin = emin;
+    res->eigmax = emax;
+    res->refinements = nref;
+    res->rel_residual = rel;
+    res->converged = rel >= 0 && rel < prm->eps;
+    return TL_OK;
+  }
   if (!ctx->host_sc->done) {
     if ((rc = tl_run_graph(ctx, exact ? TL_GRAPH_CHEBY_EXACT : TL_GRAPH_CHEBY_FAST, &ctx->last_solve_ms))) return rc;
     if ((rc = tl_read_scalars(ctx))) return rc;
