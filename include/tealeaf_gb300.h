@@ -61,6 +61,9 @@ enum {
   TL_CRIT_REFERENCE = 0,  /* each solver's own test: CG sqrt|rr| < eps (CG.jl:24), others |error| < eps */
   TL_CRIT_RELATIVE = 1    /* sqrt(rr / (u0.u0)) < eps on the recursive residual, then checked on the true one */
 };
+/* TL_PREC_FP32_IR (tealeaf mode, fused kernels): CG, and Chebyshev after its
+ * switch, iterate in FP32 inside FP64 refinement to the relative true
+ * residual; also in tl_batch_solve (CG). */
 enum { TL_PREC_FP64 = 0, TL_PREC_FP32_IR = 1 };
 
 /* Chunk(settings) (src/chunk.jl:68-89) */
