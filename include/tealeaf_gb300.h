@@ -239,6 +239,26 @@ int tl_field_summary_noalloc(const double *volume, const double *density, const 
                              int xcells, int ycells, int halodepth, long long pitch, double *out, void *stream,
                              char *err, int errlen);
 
+/* ---- the tea.in reader ---------------------------------------------------
+ * Settings(infile) (src/settings.jl:90-135) and readstate (:142-173): `text`
+ * is a deck's contents.  `deck` receives the Settings fields (the reference's
+ * defaults where the deck is silent; dx, dy from the domain); states[0..n)
+ * receive the first n = min(deck->nstates, maxstates) states with their bounds
+ * inset as `mode` tests them (reference: dx/100 with dx as it stood when the
+ * state line was read; tealeaf: the deck's final dx/100), ready for
+ * tl_initialise.  Unknown keys and values that do not parse are skipped and
+ * counted in deck->warnings, as the reference warns; a malformed state line
+ * returns TL_ERR_ARG with the message in err.  Host only: no device work. */
+typedef struct {
+  long long endstep;
+  int presteps, maxiters, coefficient, ppcginnersteps, summaryfrequency, halodepth, xcells, ycells;
+  int errorswitch, checkresult, solver;
+  double eps, dtinit, endtime, epslim, xmin, ymin, xmax, ymax, dx, dy;
+  int nstates;              /* states in the deck (may exceed maxstates) */
+  int warnings;             /* lines skipped with a warning */
+} tl_deck;
+int tl_parse_deck(const char *text, int mode, tl_deck *deck, tl_state *states, int maxstates, char *err, int errlen);
+
 /* ---- learned warm start ------------------------------------------------
  * No counterpart in the reference.  A 6-layer 3x3 convolutional network (32
  * channels, GELU between layers, BF16 weights, FP32 accumulation on the

@@ -49,6 +49,15 @@ class Result(C.Structure):
                 ("r0_plain", C.c_double), ("r0_pred", C.c_double)]
 
 
+class Deck(C.Structure):
+    """tl_deck: the Settings fields the library's tea.in reader returns."""
+    _fields_ = [("endstep", C.c_longlong)] + [(k, C.c_int) for k in (
+        "presteps", "maxiters", "coefficient", "ppcginnersteps", "summaryfrequency", "halodepth", "xcells", "ycells",
+        "errorswitch", "checkresult", "solver")] + [(k, C.c_double) for k in (
+        "eps", "dtinit", "endtime", "epslim", "xmin", "ymin", "xmax", "ymax", "dx", "dy")] + [
+        ("nstates", C.c_int), ("warnings", C.c_int)]
+
+
 class WarmCrop(C.Structure):
     """tl_warm_crop: a crop of a deck's device fields for the network kernels."""
     _fields_ = [("u", C.c_void_p), ("uprev", C.c_void_p), ("rho", C.c_void_p), ("pitch", C.c_longlong),
@@ -97,6 +106,7 @@ SIGNATURES = {
     "tl_batch_last_ms": ([C.c_void_p, _P(C.c_double)], C.c_int),
     "tl_field_summary_noalloc": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
                                   C.c_longlong, C.c_void_p, C.c_void_p, C.c_char_p, C.c_int], C.c_int),
+    "tl_parse_deck": ([C.c_char_p, C.c_int, _P(Deck), _P(State), C.c_int, C.c_char_p, C.c_int], C.c_int),
     "tl_warm_load": ([_CTX, _P(C.c_float), C.c_int], C.c_int),
     "tl_warm_reset": ([_CTX], C.c_int),
     "tl_conv3x3_forward": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -106,3 +106,41 @@ def test_library_loads_through_binding(built_lib):
 def test_julia_float_print(tl, v, text):
     """debugrecord writes floats the way Julia's print does (src/TeaLeaf.jl:90-107)."""
     assert tl._julia_repr(v) == text
+
+
+@pytest.mark.parametrize("text", DECKS)
+@pytest.mark.parametrize("mode", [0, 1])
+def test_native_deck_reader_matches_host_reader(tl, built_lib, text, mode):
+    """tl_parse_deck (the tea.in reader inside the library, no device work)
+    against the host reader: every Settings field, the warning count, and
+    each state's inset bounds as the given semantics tests them."""
+    import warnings as W
+    lib = tl._abi.load()
+    deck = tl._abi.Deck()
+    states = (tl._abi.State * 16)()
+    err = C.create_string_buffer(256)
+    assert lib.tl_parse_deck(text.encode(), mode, C.byref(deck), states, 16, err, 256) == 0, err.value
+    with W.catch_warnings(record=True) as caught:
+        W.simplefilter("always")
+        s = tl.Settings.from_text(text)
+    assert deck.warnings == len(caught)
+    for k in INT_KEYS + ["coefficient", "solver"]:
+        assert getattr(deck, k) == getattr(s, k), k
+    assert bool(deck.errorswitch) == s.errorswitch and bool(deck.checkresult) == s.checkresult
+    for k in F_KEYS:
+        assert getattr(deck, k) == getattr(s, k), k
+    assert deck.nstates == len(s.states)
+    for k, st in enumerate(s.states):
+        b = st.bounds(s, mode)
+        got = states[k]
+        assert (got.density, got.energy, got.radius, got.geometry) == (st.density, st.energy, st.radius, st.geometry)
+        assert (got.xmin, got.ymin, got.xmax, got.ymax) == b
+
+
+def test_native_deck_reader_rejects_malformed_state(tl, built_lib):
+    lib = tl._abi.load()
+    deck = tl._abi.Deck()
+    err = C.create_string_buffer(256)
+    for bad in ("state 2 density=1.0 energy 3\n", "state 2 density=1.0 geometry=hexagon\n", "state x density=1\n"):
+        assert lib.tl_parse_deck(bad.encode(), 1, C.byref(deck), None, 0, err, 256) == tl._abi.ERR_ARG
+        assert err.value
