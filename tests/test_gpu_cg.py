@@ -195,3 +195,38 @@ def test_debugrecord_dump(tl, built_lib, tmp_path):
             assert vals == list(a[:, j])
         assert lines[pos + 1 + Y] == ""
         pos += Y + 2
+
+
+@pytest.mark.parametrize("mode,precision,criterion", [(REF, 0, 0), (TEA, 0, 0), (TEA, 1, 1)])
+def test_c_driver_matches_host_mirror(tl, built_lib, tmp_path, mode, precision, criterion):
+    """The plain C driver (tests/c_driver.c: the library's deck reader, then
+    tl_diffuse) on config 1 gives the host mirror's summaries and iteration
+    counts: bit-identical in FP64, within the refinement's tolerance in FP32."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+    if not shutil.which("gcc"):
+        pytest.skip("no gcc")
+    root = Path(__file__).resolve().parents[1]
+    lib = Path(built_lib)
+    exe = tmp_path / "c_driver"
+    subprocess.run(["gcc", "-std=c99", "-O1", "-I", str(root / "include"), str(root / "tests" / "c_driver.c"),
+                    "-o", str(exe), str(lib), f"-Wl,-rpath,{lib.parent}"], check=True)
+    deck = tmp_path / "tea.in"
+    text = CONFIG1 if precision == 0 else deck_text(eps=1e-10)
+    deck.write_text(text)
+    out = subprocess.run([str(exe), str(deck), str(mode), str(precision), str(criterion), "0"], check=True,
+                         capture_output=True, text=True).stdout.split("\n")
+    sums = [tuple(float(x) for x in ln.split()[1:]) for ln in out if ln.startswith("summary")]
+    iters = [int(x) for ln in out if ln.startswith("iters") for x in ln.split()[1:]]
+    s = tl.Settings.from_text(text, mode=mode, precision=precision, criterion=criterion)
+    chunk = tl.initialiseapp(s)
+    steps, hsums = tl.diffuse(chunk, s, problemfile=None)
+    assert len(iters) == len(steps) and sums
+    if precision == 0:
+        assert iters == [r.iters for r in steps]
+        assert sums[-1] == tuple(hsums[-1])
+    else:
+        assert all(abs(a - b) <= max(3, 0.05 * b) for a, b in zip(iters, [r.iters for r in steps]))
+        for x, y in zip(sums[-1], hsums[-1]):
+            assert rel(x, y) <= 1e-9

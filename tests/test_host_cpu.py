@@ -144,3 +144,18 @@ def test_native_deck_reader_rejects_malformed_state(tl, built_lib):
     for bad in ("state 2 density=1.0 energy 3\n", "state 2 density=1.0 geometry=hexagon\n", "state x density=1\n"):
         assert lib.tl_parse_deck(bad.encode(), 1, C.byref(deck), None, 0, err, 256) == tl._abi.ERR_ARG
         assert err.value
+
+
+def test_c_driver_compiles_against_the_header(built_lib, tmp_path):
+    """The header is plain C: a C driver that uses the deck reader, the
+    context, tl_diffuse and the summaries compiles and links with gcc."""
+    import shutil
+    import subprocess
+    if not shutil.which("gcc"):
+        pytest.skip("no gcc")
+    lib = Path(built_lib)
+    exe = tmp_path / "c_driver"
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", str(ROOT / "include"),
+                    str(ROOT / "tests" / "c_driver.c"), "-o", str(exe), str(lib), f"-Wl,-rpath,{lib.parent}"],
+                   check=True)
+    assert exe.exists()
