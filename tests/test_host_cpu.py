@@ -159,3 +159,19 @@ def test_c_driver_compiles_against_the_header(built_lib, tmp_path):
                     str(ROOT / "tests" / "c_driver.c"), "-o", str(exe), str(lib), f"-Wl,-rpath,{lib.parent}"],
                    check=True)
     assert exe.exists()
+
+
+@pytest.mark.parametrize("cfg,code", [((0, 10, 2, 100, 0), 1), ((10, 10, 0, 100, 1), 1), ((10, 10, 2, 0, 1), 1),
+                                       ((10, 10, 2, 100, 7), 1), ((10, 12, 2, 100, 0), 5)])
+def test_create_rejects_invalid_configurations(tl, built_lib, cfg, code):
+    """tl_create validates before touching the device: non-positive sizes,
+    halo depth or table length, an unknown mode (TL_ERR_ARG); a non-square
+    deck in reference mode raises like Chunk (src/chunk.jl:44)."""
+    lib = tl._abi.load()
+    nx, ny, hd, maxiters, mode = cfg
+    c = tl._abi.Config(nx, ny, hd, maxiters, 0.0, 0.0, 1.0, 1.0, mode)
+    ctx = C.c_void_p()
+    rc = lib.tl_create(C.byref(ctx), C.byref(c))
+    msg = lib.tl_last_error(ctx)
+    lib.tl_destroy(ctx)
+    assert rc == code and msg
