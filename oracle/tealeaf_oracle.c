@@ -687,9 +687,14 @@ int tlo_cg_init(tlo_chunk *c, int coefficient, double rx, double ry, const tlo_o
          *w = c->f[TLO_W], *kx = c->f[TLO_KX], *ky = c->f[TLO_KY];
 #pragma omp parallel for num_threads(NT(o)) schedule(static)
   for (size_t k = 0; k < n; ++k) { u[k] = e[k] * rho[k]; p[k] = 0.0; r[k] = 0.0; }
+  /* CG.jl:57-60 computes w on 2:X-1 x 2:Y-1 only; with halo depth 1 the
+   * outer halo layer then keeps w = 0 and Kx, Ky at the domain edge are
+   * infinite.  Tealeaf mode computes w over the whole array (the density
+   * halo is exchanged), which changes nothing for halo depth >= 2. */
+  const int w0 = o->mode == TLO_MODE_TEALEAF ? 0 : 1;
 #pragma omp parallel for num_threads(NT(o)) schedule(static)
-  for (int j = 1; j < Y - 1; ++j)
-    for (int i = 1; i < X - 1; ++i)
+  for (int j = w0; j < Y - w0; ++j)
+    for (int i = w0; i < X - w0; ++i)
       w[IDX(i, j)] = coefficient == TLO_CONDUCTIVITY ? rho[IDX(i, j)] : 1.0 / rho[IDX(i, j)];
 #pragma omp parallel for num_threads(NT(o)) schedule(static)
   for (int j = hd; j < Y - 1; ++j)

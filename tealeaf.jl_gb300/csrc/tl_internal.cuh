@@ -91,7 +91,7 @@ void launch_copy_full(cudaStream_t st, double *dst, const double *src, const Geo
 // halo of up to 6 fields; `fields` holds device pointers
 void launch_halo(cudaStream_t st, double *const *fields, int nf, const Geom &g, int depth, int mode);
 
-void launch_init_pre(cudaStream_t st, const Fields &F, const Geom &g, int coefficient);
+void launch_init_pre(cudaStream_t st, const Fields &F, const Geom &g, int coefficient, int mode);
 void launch_init_coef(cudaStream_t st, const Fields &F, const Geom &g, double rx, double ry, int from_density,
                       int coefficient);
 void launch_init_diag(cudaStream_t st, const Fields &F, const Geom &g);

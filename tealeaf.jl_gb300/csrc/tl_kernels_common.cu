@@ -168,7 +168,11 @@ void launch_halo(cudaStream_t st, double *const *fields, int nf, const Geom &g, 
 // ---------------------------------------------------------------------------
 
 // u = energy*density, p = r = 0 on the whole array; w = density^(+-1) on halo(1).
-__global__ void k_init_pre(Fields F, Geom g, int coefficient) {
+// CG.init! (CG.jl:53-60): u = energy * density, p = r = 0, w = density^(+-1)
+// on 2:X-1 x 2:Y-1.  With halo depth 1 that range leaves w = 0 in the outer
+// halo layer and Kx, Ky at the domain edge infinite; tealeaf mode (w0 = 0)
+// computes w over the whole array, which changes nothing for depth >= 2.
+__global__ void k_init_pre(Fields F, Geom g, int coefficient, int w0) {
   const long long n = (long long)g.X * g.Y;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
     const int I = (int)(k % g.X), J = (int)(k / g.X);
@@ -177,13 +181,14 @@ __global__ void k_init_pre(Fields F, Geom g, int coefficient) {
     F.u[c] = dmul(F.energy[c], rho);
     F.p[c] = 0.0;
     F.r[c] = 0.0;
-    if (I >= 1 && I < g.X - 1 && J >= 1 && J < g.Y - 1)
+    if (I >= w0 && I < g.X - w0 && J >= w0 && J < g.Y - w0)
       F.w[c] = (coefficient == TL_CONDUCTIVITY) ? rho : ddiv(1.0, rho);
   }
 }
 
-void launch_init_pre(cudaStream_t st, const Fields &F, const Geom &g, int coefficient) {
-  k_init_pre<<<grid_for((long long)g.X * g.Y, 256), 256, 0, st>>>(F, g, coefficient);
+void launch_init_pre(cudaStream_t st, const Fields &F, const Geom &g, int coefficient, int mode) {
+  k_init_pre<<<grid_for((long long)g.X * g.Y, 256), 256, 0, st>>>(F, g, coefficient,
+                                                                   mode == TL_MODE_TEALEAF ? 0 : 1);
 }
 
 // kx, ky over [hd, X-1) x [hd, Y-1): rx*(wl + wc)/(2*wl*wc).  from_density

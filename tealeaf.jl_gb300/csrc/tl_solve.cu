@@ -61,7 +61,7 @@ int tl_cg_init(tl_ctx *ctx, double rx, double ry, int coefficient, int exact) {
     tl_set_error(ctx, "Coefficient %d is not valid (src/solvers/CG.jl:49)", coefficient);
     return TL_ERR_COEF;
   }
-  launch_init_pre(ctx->stream, ctx->F, ctx->g, coefficient);
+  launch_init_pre(ctx->stream, ctx->F, ctx->g, coefficient, ctx->cfg.mode);
   CKL();
   launch_init_coef(ctx->stream, ctx->F, ctx->g, rx, ry, 0, coefficient);
   CKL();
@@ -344,6 +344,22 @@ int tl_cg_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_resu
   ctx->launches += 3;
   if (prm->warmstart && (rc = tl_warm_try(ctx, rx, ry, prm->warmstart, res))) return rc;
   ctx->last_solve_ms = 0.0;
+  if (prm->criterion == TL_CRIT_RELATIVE) {
+    // the relative test also holds before the first iteration (an exact
+    // start, where CG's alpha would be 0/0)
+    if ((rc = tl_read_scalars(ctx))) return rc;
+    const DevScalars &s0 = *ctx->host_sc;
+    const double rel0 = s0.bb > 0 ? sqrt(s0.rro / s0.bb) : sqrt(s0.rro);
+    if (rel0 < prm->eps) {
+      res->iters = res->cg_iters = 0;
+      res->error = s0.rro;
+      res->converged = 1;
+      res->rel_residual = rel0;
+      res->launches = (int)ctx->launches;
+      if (prm->warmstart) tl_warm_after(ctx, res, prm->warmstart);
+      return TL_OK;
+    }
+  }
   const int which = ref ? TL_GRAPH_CG_REF : (exact ? TL_GRAPH_CG_EXACT : TL_GRAPH_CG_FAST);
   double rel = -1.0;
   int ran = 0;

@@ -167,8 +167,12 @@ def cg_init(ch, hd, coef, rx, ry, intended):
         ch.u.a[k] = ch.energy.a[k] * ch.density.a[k]
         ch.p.a[k] = 0.0
         ch.r.a[k] = 0.0
-    for j in range(2, ch.y):
-        for i in range(2, ch.x):
+    # CG.jl:57-60 fills w on 2:X-1 x 2:Y-1; the intended algorithm fills the
+    # whole array (with halo depth 1 the 2:X-1 range leaves w = 0 in the halo
+    # and Kx, Ky at the domain edge infinite)
+    lo, hi_x, hi_y = (1, ch.x + 1, ch.y + 1) if intended else (2, ch.x, ch.y)
+    for j in range(lo, hi_y):
+        for i in range(lo, hi_x):
             ch.w[i, j] = ch.density[i, j] if coef == 1 else 1.0 / ch.density[i, j]
     for jj in range(hd + 1, ch.y):
         for kk in range(hd + 1, ch.x):

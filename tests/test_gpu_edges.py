@@ -1,7 +1,12 @@
 """GPU edge cases of the solve path against the CPU oracle: one-cell and
 one-cell-wide decks, halo depths other than 2, iteration caps that end the
 loop, and a tolerance met at once.  Bit-identical to the oracle in the device
-order where the kernels take the reference operation order (`exact`)."""
+order where the kernels take the reference operation order (`exact`).
+
+A one-cell deck is exact at the start: r = 0 and CG's alpha is 0/0, so the
+reference's loop (and both semantics with its own test) runs to max_iters
+on NaN; that is compared as it is.  The relative test stops before the first
+iteration instead (see test_fp32_refined_tiny_decks)."""
 import numpy as np
 import pytest
 
@@ -16,14 +21,20 @@ def _deck(nx, ny, seed=9, **kv):
     return random_deck(nx, seed, ny=ny, nrect=3, steps=2, eps=1e-12, **kv)
 
 
+def _eq(a, b):
+    """Equal, with NaN equal to NaN."""
+    return np.array_equal(np.asarray(a, dtype=float), np.asarray(b, dtype=float), equal_nan=True)
+
+
 def _same(tl, text, mode):
     chunk, res, sums, per = gpu_run(tl, text, mode, exact=True, steps_fields=True)
     _, ores, osums, oper = oracle_run(text, mode, O.ORDER_DEVICE, chunk.reduction_layout(), steps_fields=True)
-    assert [(r.iters, r.error) for r in res] == [(r.iters, r.error) for r in ores]
+    assert [r.iters for r in res] == [r.iters for r in ores]
+    assert _eq([r.error for r in res], [r.error for r in ores])
     for f in FIELDS:
         np.testing.assert_array_equal(per[-1][f], oper[-1][f], err_msg=f)
     for g, o in zip(sums, osums):
-        assert tuple(g) == tuple(o)
+        assert _eq(g, o)
     return res
 
 
@@ -36,7 +47,10 @@ def test_tiny_and_thin_decks(tl, built_lib, nx, ny):
 
 @pytest.mark.parametrize("hd", [1, 3, 4])
 def test_halo_depths_tealeaf(tl, built_lib, hd):
-    _same(tl, _deck(24, 20, halo_depth=hd), TEA)
+    """Tealeaf mode computes w over the whole array, so halo depth 1 keeps
+    Kx, Ky at the domain edge finite (the reference's 2:X-1 range does not)."""
+    res = _same(tl, _deck(24, 20, halo_depth=hd), TEA)
+    assert all(r.converged and np.isfinite(r.error) for r in res)
 
 
 def test_halo_depth_1_reference_raises(tl, built_lib):
