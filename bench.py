@@ -427,7 +427,8 @@ def run_config2(args):
     n = args.size if args.size != 8192 else 4096
     peak, peak_kind = measured_peaks()
     out = {"workload": f"config2: 5-state geometry on {n}^2, 10 steps, eps 1e-10", "n": n, "solvers": {}}
-    for solver in ("cg", "cheby", "ppcg"):
+    chosen = [x for x in args.solvers.split(",") if x]
+    for solver in [x for x in ("cg", "cheby", "ppcg") if x in chosen]:
         runs = []
         chunk = None
         for run in range(3):
@@ -455,7 +456,7 @@ def run_config2(args):
     # the same decks to the relative true residual 1e-10: FP64 and FP32 inside
     # FP64 refinement, CG and Chebyshev (one run each)
     out["relative"] = {}
-    for solver in ("cg", "cheby"):
+    for solver in [x for x in ("cg", "cheby") if x in chosen]:
         for prec, pname in ((0, "fp64"), (1, "fp32_refined")):
             s = tl.Settings.from_text(config2_deck(n, solver), mode=1, exact=False, criterion=1, precision=prec)
             chunk = tl.initialiseapp(s)
@@ -488,7 +489,7 @@ def run_config2(args):
             ch.solve(s.dtinit / s.dx ** 2, s.dtinit / s.dy ** 2)
             t[cap] = time.perf_counter() - t0
         per_iter = (t[25] - t[5]) / 20
-        cg_iters = sum(out["solvers"]["cg"]["runs"][0]["iters"])
+        cg_iters = sum(out["solvers"]["cg"]["runs"][0]["iters"]) if "cg" in out["solvers"] else 0
         out["cpu_cg"] = {"ms_per_iteration": per_iter * 1e3, "cores": threads, "kind": "port",
                          "estimated_ms_per_run": per_iter * 1e3 * cg_iters}
     print(json.dumps(out))
@@ -659,6 +660,7 @@ def main():
                          "config4: 128 uneven decks, batched against sequential; config5: the learned warm "
                          "start (kernel rates, training step, A/B evaluation; --size, --steps)")
     ap.add_argument("--no-eval", action="store_true", help="config5: kernel rates and training step only")
+    ap.add_argument("--solvers", default="cg,cheby,ppcg", help="config2: the solvers to run (comma list)")
     ap.add_argument("--decks", type=int, default=128)
     args = ap.parse_args()
     if args.warmup < 3:
