@@ -320,6 +320,24 @@ struct OpCheby32 {
   __device__ bool skip() const { return guard && F.sc->done; }
   __device__ void on_skip() const {}
 
+  // The per-row operands other than e, loaded one row ahead of their use.
+  struct Row {
+    float4 kx, r0, p;
+    float ew, ee, kxe;  // west edge (lane 0), east edge and its kx (lane 31 or the last column)
+  };
+  __device__ __forceinline__ void load_row(Row &o, int i0, int j, bool valid, bool full, bool inner, int lane) const {
+    if (!valid) return;
+    const size_t c = g.at(i0, j);
+    o.kx = ld4(q.kx + c);
+    o.r0 = ld4(q.r + c);
+    o.p = ld4(p + c);
+    if (lane == 0 && i0 > 0) o.ew = __ldg(esrc + c - 1);
+    if (full && (lane == 31 || !inner)) {
+      o.kxe = __ldg(q.kx + c + 4);
+      if (inner) o.ee = __ldg(esrc + c + 4);
+    }
+  }
+
   __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
     const int nx = g.nx, ny = g.ny;
     const int lane = threadIdx.x & 31;
@@ -334,23 +352,28 @@ struct OpCheby32 {
     auto ld = [&](const float *a, int j) { return valid ? ld4(a + g.at(i0, j)) : z; };
     float4 ec = ld(esrc, j0);
     float4 es = j0 > 0 ? ld(esrc, j0 - 1) : ec;
-    float4 kys = ld(q.ky, j0);
-    float a = 0.f;
+    float4 en = j0 + 1 < ny ? ld(esrc, j0 + 1) : ec;
+    float4 kys = ld(q.ky, j0), kyn = ld(q.ky, j0 + 1);
+    Row cur = {}, nxt = {};
+    load_row(cur, i0, j0, valid, full, inner, lane);
     for (int j = j0; j < j1; ++j) {
-      const float4 en = j + 1 < ny ? ld(esrc, j + 1) : ec;
-      const float4 kyn = ld(q.ky, j + 1);
-      const float4 kx = ld(q.kx, j);
-      const float4 r0 = ld(q.r, j);
-      const float4 pv = ld(p, j);
+      // next row's operands, and e and ky two rows ahead
+      float4 enn = z, kynn = z;
+      if (j + 1 < j1) {
+        load_row(nxt, i0, j + 1, valid, full, inner, lane);
+        if (j + 2 < ny) enn = ld(esrc, j + 2);
+        kynn = ld(q.ky, j + 2);
+      }
       float ew = __shfl_up_sync(FULL, ec.w, 1);
       float ee = __shfl_down_sync(FULL, ec.x, 1);
-      float kxe = __shfl_down_sync(FULL, kx.x, 1);
+      float kxe = __shfl_down_sync(FULL, cur.kx.x, 1);
+      float a = 0.f;
       if (valid) {
         if (i0 == 0) ew = ec.x;
-        else if (lane == 0) ew = __ldg(esrc + g.at(i0 - 1, j));
+        else if (lane == 0) ew = cur.ew;
         if (full && (lane == 31 || !inner)) {
-          kxe = __ldg(q.kx + g.at(i0 + 4, j));
-          ee = inner ? __ldg(esrc + g.at(i0 + 4, j)) : ec.w;
+          kxe = cur.kxe;
+          ee = inner ? cur.ee : ec.w;
         }
         float pn[4], en4[4];
 #pragma unroll
@@ -361,14 +384,14 @@ struct OpCheby32 {
             const float c = comp(ec, m);
             const float e = (m + 1 < ncell) ? comp(ec, m + 1) : (m == 3 ? ee : c);
             const float wl = (m == 0) ? ew : comp(ec, m - 1);
-            const float k1 = (m == 3) ? kxe : comp(kx, m + 1);
+            const float k1 = (m == 3) ? kxe : comp(cur.kx, m + 1);
             float w = c;
             w = fmaf(k1, c - e, w);
-            w = fmaf(comp(kx, m), c - wl, w);
+            w = fmaf(comp(cur.kx, m), c - wl, w);
             w = fmaf(comp(kyn, m), c - comp(en, m), w);
             w = fmaf(comp(kys, m), c - comp(es, m), w);
-            const float r = comp(r0, m) - w;
-            pn[m] = fmaf(ca, comp(pv, m), cb * r);
+            const float r = comp(cur.r0, m) - w;
+            pn[m] = fmaf(ca, comp(cur.p, m), cb * r);
             en4[m] = c + pn[m];
             a = fmaf(r, r, a);
           }
@@ -385,10 +408,12 @@ struct OpCheby32 {
         }
       }
       acc[0] += (double)a;
-      a = 0.f;
       es = ec;
       ec = en;
+      en = (j + 2 < ny) ? enn : ec;
       kys = kyn;
+      kyn = kynn;
+      cur = nxt;
     }
   }
   __device__ void fin(const double *tot) const {
