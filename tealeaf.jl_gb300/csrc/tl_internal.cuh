@@ -63,6 +63,7 @@ struct DevScalars {
   int pbuf;             // 1: the current FP32 search direction is in the second buffer
   int finished;         // the deck's solve is over (converged or out of iterations)
   int refinements;      // FP64 refinement steps taken
+  int prestep_switch;   // FP32 CG presteps of Chebyshev: the switch test held (Cheby.jl:25-29)
 };
 
 // Device pointers of one context, passed to kernels by value.

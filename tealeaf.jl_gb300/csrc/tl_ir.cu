@@ -190,34 +190,26 @@ static int refine(tl_ctx *ctx, double *rr, float *e = nullptr) {
   return TL_OK;
 }
 
-int tl_ir_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res) {
-  if (ctx->cfg.mode != TL_MODE_TEALEAF) {
-    tl_set_error(ctx, "FP32 refinement needs the tealeaf (5-point) semantics");
-    return TL_ERR_ARG;
-  }
-  int rc = ensure_ir(ctx);
-  if (rc) return rc;
-  tl_params p = *prm;
-  p.criterion = TL_CRIT_RELATIVE;
-  if ((rc = tl_cg_init(ctx, rx, ry, p.coefficient, 1))) return rc;
-  if ((rc = tl_set_loop_params(ctx, &p, 0, 0))) return rc;
-  const int up[2] = {TL_EX_U, TL_EX_P};
-  if ((rc = tl_halo_update(ctx, 1, up, 2, 1))) return rc;
-  if ((rc = tl_copy_u(ctx))) return rc;
-  if (prm->warmstart && (rc = tl_warm_try(ctx, rx, ry, prm->warmstart, res))) return rc;
+// The inner loop with its refinements, from the state tl_cg_init and copyu
+// left (u, r = p = u0 - A u, r.r in rro).  Runs until the relative true
+// residual is below eps, the iteration budget is spent or, as CG presteps of
+// Chebyshev (switch rule 1), the switch test held; the FP32 search direction
+// is exported into p.  Returns the last true r.r and its relative value.
+static int ir_loop(tl_ctx *ctx, const tl_params &p, double *rr_out, double *rel_out, int *refinements) {
   const G32 g32 = g32_of(ctx);
   tl_ir_state *ir = ctx->ir;
   k_ir_convert<<<grid_for((long long)ctx->g.X * ctx->g.Y), 256, 0, ctx->stream>>>(ctx->F, ctx->g, g32, ir->kx, ir->ky,
                                                                                   ir->r, ir->p, ir->x);
   CKL();
   ctx->launches += 8;
-  if ((rc = tl_read_scalars(ctx))) return rc;
+  int rc = tl_read_scalars(ctx);
+  if (rc) return rc;
   const double bb = ctx->host_sc->bb;
   double rr = ctx->host_sc->rro;
   double rel = bb > 0 ? sqrt(rr / bb) : sqrt(rr);
-  int which = 0, refinements = 0;
+  int which = 0, nref = 0, switched = 0;
   ctx->last_solve_ms = 0.0;
-  while (rel >= p.eps && ctx->host_sc->iter < p.maxiters) {
+  while (rel >= p.eps && ctx->host_sc->iter < p.maxiters && !switched) {
     k_ir_start<<<1, 1, 0, ctx->stream>>>(ctx->F.sc, rr, IR_DELTA * IR_DELTA);
     CKL();
     cudaGraphExec_t exec = nullptr;
@@ -248,18 +240,44 @@ int tl_ir_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_resu
     ctx->last_solve_ms += t;
     if ((rc = tl_read_scalars(ctx))) return rc;
     const int trips = ctx->host_sc->iter - before;
+    switched = ctx->host_sc->prestep_switch;
     ctx->launches += 1 + 4LL * ((trips + 1) / 2);
     if (trips & 1) which ^= 1;  // the last step wrote p into the other buffer
     if ((rc = refine(ctx, &rr))) return rc;
-    ++refinements;
+    ++nref;
     rel = bb > 0 ? sqrt(rr / bb) : sqrt(rr);
   }
   float *pcur = which ? ir->pb : ir->p;
   k_ir_export_p<<<grid_for((long long)ctx->g.nx * ctx->g.ny), 256, 0, ctx->stream>>>(ctx->F, ctx->g, g32, pcur);
   CKL();
+  const int up[2] = {TL_EX_U, TL_EX_P};
   if ((rc = tl_halo_update(ctx, 1, up, 2, 1))) return rc;
   ctx->launches += 2;
   if ((rc = tl_read_scalars(ctx))) return rc;
+  *rr_out = rr;
+  *rel_out = rel;
+  *refinements = nref;
+  return TL_OK;
+}
+
+int tl_ir_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res) {
+  if (ctx->cfg.mode != TL_MODE_TEALEAF) {
+    tl_set_error(ctx, "FP32 refinement needs the tealeaf (5-point) semantics");
+    return TL_ERR_ARG;
+  }
+  int rc = ensure_ir(ctx);
+  if (rc) return rc;
+  tl_params p = *prm;
+  p.criterion = TL_CRIT_RELATIVE;
+  if ((rc = tl_cg_init(ctx, rx, ry, p.coefficient, 1))) return rc;
+  if ((rc = tl_set_loop_params(ctx, &p, 0, 0))) return rc;
+  const int up[2] = {TL_EX_U, TL_EX_P};
+  if ((rc = tl_halo_update(ctx, 1, up, 2, 1))) return rc;
+  if ((rc = tl_copy_u(ctx))) return rc;
+  if (prm->warmstart && (rc = tl_warm_try(ctx, rx, ry, prm->warmstart, res))) return rc;
+  double rr = 0.0, rel = 0.0;
+  int refinements = 0;
+  if ((rc = ir_loop(ctx, p, &rr, &rel, &refinements))) return rc;
   res->iters = ctx->host_sc->iter;
   res->cg_iters = ctx->host_sc->iter;
   res->error = rr;
@@ -268,6 +286,34 @@ int tl_ir_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_resu
   res->refinements = refinements;
   res->launches = (int)ctx->launches;
   if (prm->warmstart) tl_warm_after(ctx, res, prm->warmstart);
+  return TL_OK;
+}
+
+// The CG presteps of Chebyshev (Cheby.jl:15-35, tealeaf mode) as FP32 inner
+// sweeps inside FP64 refinement.  The FP32 epilogues record alpha and beta in
+// the coefficient tables for the eigenvalue estimate and apply the switch
+// test (Cheby.jl:25-29) to the inner r.r; when it holds, the correction is
+// folded into u and the true residual measured before the Chebyshev phase
+// takes over.  On return u (with its halo) is the iterate, the host scalars
+// hold the loop's end state, *switched says whether the Chebyshev phase takes
+// over (the switch test held and the true residual is not yet below eps) and
+// *rel_out is the relative true residual.
+int tl_ir_presteps(tl_ctx *ctx, double rx, double ry, const tl_params *prm, int *refinements, double *rel_out,
+                   int *switched) {
+  int rc = ensure_ir(ctx);
+  if (rc) return rc;
+  tl_params p = *prm;
+  p.criterion = TL_CRIT_RELATIVE;
+  // exact 0: the stored diagonal, which the FP64 Chebyshev steps after the
+  // switch read
+  if ((rc = tl_cg_init(ctx, rx, ry, p.coefficient, 0))) return rc;
+  if ((rc = tl_set_loop_params(ctx, &p, 1, 0))) return rc;
+  const int up[2] = {TL_EX_U, TL_EX_P};
+  if ((rc = tl_halo_update(ctx, 1, up, 2, 1))) return rc;
+  if ((rc = tl_copy_u(ctx))) return rc;
+  double rr = 0.0;
+  if ((rc = ir_loop(ctx, p, &rr, rel_out, refinements))) return rc;
+  *switched = ctx->host_sc->prestep_switch && *rel_out >= p.eps;
   return TL_OK;
 }
 

@@ -194,6 +194,9 @@ struct OpIrW {
     DevScalars *sc = F.sc;
     sc->pw = tot[0];
     sc->alpha = sc->rro / sc->pw;
+    // as CG presteps of Chebyshev, the coefficient table for the eigenvalue
+    // estimate (CG.jl:37; 1-based, maxiters + 2 entries)
+    if (sc->switch_rule == 1 && sc->iter < sc->maxiters) F.cgalpha[sc->iter + 1] = sc->alpha;
   }
 };
 
@@ -245,6 +248,14 @@ struct OpIrUR {
     DevScalars *sc = F.sc;
     const double rrn = tot[0];
     sc->beta = rrn / sc->rro;
+    bool sw = false;
+    if (sc->switch_rule == 1) {
+      // CG presteps of Chebyshev: the beta table and the switch test
+      // (Cheby.jl:25-29) on this step's r.r
+      if (sc->iter < sc->maxiters) F.cgbeta[sc->iter + 1] = sc->beta;
+      const int tt = sc->iter + 2;  // the solver loop's next trip
+      sw = sc->errorswitch ? (rrn < sc->epslim && tt > CGEIGENITERS) : (tt > sc->presteps && rrn < ERROR_SWITCH_MAX);
+    }
     sc->rro = rrn;
     sc->error = rrn;
     sc->iter += 1;
@@ -253,7 +264,8 @@ struct OpIrUR {
     const bool refine = claim || rrn < sc->delta2 * sc->rr_ref;
     sc->converged = 0;
     sc->switched = refine;
-    const int done = refine || sc->iter >= sc->maxiters;
+    sc->prestep_switch = sw;
+    const int done = refine || sw || sc->iter >= sc->maxiters;
     sc->done = done;
     if (set_cond) cudaGraphSetConditional(cond, done ? 0u : 1u);
   }
@@ -331,6 +343,7 @@ __global__ void k_ir_start(DevScalars *sc, double rr, double delta2) {
   sc->delta2 = delta2;
   sc->done = 0;
   sc->switched = 0;
+  sc->prestep_switch = 0;
 }
 
 G32 g32_of(tl_ctx *ctx) {

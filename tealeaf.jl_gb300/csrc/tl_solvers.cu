@@ -274,14 +274,31 @@ static void fill_result(tl_ctx *ctx, tl_result *res, int cg_iters) {
 int tl_cheby_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res) {
   const int ref = ctx->cfg.mode == TL_MODE_REFERENCE;
   const int exact = ref || prm->exact;
-  int rc = cg_phase(ctx, rx, ry, prm, exact, ref ? 1 : 0);  // Cheby.jl:33 passes the init rro
-  if (rc) return rc;
-  const DevScalars sc0 = *ctx->host_sc;
-  if (!sc0.switched) {  // converged or out of iterations during the presteps
-    fill_result(ctx, res, sc0.iter);
-    res->error = prm->maxiters >= 1 ? sc0.error : ERROR_START;
-    return TL_OK;
+  // FP32 inner sweeps inside FP64 refinement, for the presteps and the
+  // Chebyshev steps (tealeaf mode; exact implies FP64)
+  const int fp32 = prm->precision == TL_PREC_FP32_IR && !exact;
+  int rc, pre_ref = 0;
+  if (fp32) {
+    double rel = -1.0;
+    int sw = 0;
+    if ((rc = tl_ir_presteps(ctx, rx, ry, prm, &pre_ref, &rel, &sw))) return rc;
+    if (!sw) {  // converged or out of iterations during the presteps
+      fill_result(ctx, res, ctx->host_sc->iter);
+      res->refinements = pre_ref;
+      res->rel_residual = rel;
+      res->converged = rel >= 0 && rel < prm->eps;
+      return TL_OK;
+    }
+  } else {
+    if ((rc = cg_phase(ctx, rx, ry, prm, exact, ref ? 1 : 0))) return rc;  // Cheby.jl:33 passes the init rro
+    const DevScalars sc0 = *ctx->host_sc;
+    if (!sc0.switched) {  // converged or out of iterations during the presteps
+      fill_result(ctx, res, sc0.iter);
+      res->error = prm->maxiters >= 1 ? sc0.error : ERROR_START;
+      return TL_OK;
+    }
   }
+  const DevScalars sc0 = *ctx->host_sc;
   if (ref) {
     res->iters = sc0.iter + 1;
     res->cg_iters = sc0.iter;
@@ -306,7 +323,7 @@ int tl_cheby_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_r
   const int est = calciter(emin, emax, ctx->host_sc->error, ctx->host_sc->bb);
   k_set_est<<<1, 1, 0, ctx->stream>>>(ctx->F.sc, est);
   CKL();
-  if (!ctx->host_sc->done && prm->precision == TL_PREC_FP32_IR && !exact) {
+  if (!ctx->host_sc->done && fp32) {
     // the rest of the iteration in FP32 inside FP64 refinement
     int nref = 0;
     double rel = -1.0;
@@ -319,7 +336,7 @@ int tl_cheby_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_r
     res->est_iters = est;
     res->eigmin = emin;
     res->eigmax = emax;
-    res->refinements = nref;
+    res->refinements = pre_ref + nref;
     res->rel_residual = rel;
     res->converged = rel >= 0 && rel < prm->eps;
     return TL_OK;

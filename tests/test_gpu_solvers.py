@@ -107,20 +107,28 @@ def test_reference_mode_raises(tl, built_lib, solver, msg, n, seed, pre):
 
 @pytest.mark.parametrize("n,seed,pre", [(128, 50, 20), (200, 51, 30)])
 def test_cheby_fp32_refined(tl, built_lib, n, seed, pre):
-    """Chebyshev after its switch in FP32 inside FP64 refinement: every step
-    meets the 1e-10 relative true residual, with at least one refinement,
-    and the final u matches FP64 Chebyshev to 1e-8 of its maximum; the
-    Chebyshev iteration counts stay within 25 % of FP64's (FP64 tests the
-    norm every 10th step past its estimate, FP32 every step)."""
+    """Chebyshev in FP32 inside FP64 refinement, the CG presteps included:
+    every step meets the 1e-10 relative true residual, with at least one
+    refinement, and the final u matches FP64 Chebyshev to 1e-8 of its
+    maximum.  The FP32 presteps record the CG coefficients for the
+    eigenvalue estimate and switch within a few iterations of FP64's (the
+    switch test reads the FP32 recurrence r.r); at the same switch the
+    estimates agree to 1e-4 relative, and the Chebyshev iteration counts to
+    25 % (FP64 tests the norm every 10th step past its estimate, FP32 every
+    step)."""
     text = random_deck(n, seed, steps=3, eps=1e-10, solver="cheby", presteps=pre)
     _, r64, _, per64 = gpu_run(tl, text, TEA, exact=False, steps_fields=True, criterion=1, precision=0)
     _, r32, _, per32 = gpu_run(tl, text, TEA, exact=False, steps_fields=True, criterion=1, precision=1)
     for tt, (a, b) in enumerate(zip(r32, r64)):
         assert a.converged and 0 <= a.rel_residual < 1e-10, (tt, a)
         assert b.converged
-        assert a.cg_iters == b.cg_iters
+        assert a.refinements >= 1
+        assert abs(a.cg_iters - b.cg_iters) <= 0.05 * b.cg_iters + 2, (tt, a.cg_iters, b.cg_iters)
         if a.inner_iters:
-            assert a.refinements >= 1
+            assert a.cg_iters >= pre
+            if a.cg_iters == b.cg_iters:
+                for x, y in ((a.eigmin, b.eigmin), (a.eigmax, b.eigmax)):
+                    assert abs(x - y) <= 1e-4 * abs(y), (tt, a.eigmin, a.eigmax, b.eigmin, b.eigmax)
             assert abs(a.inner_iters - b.inner_iters) <= 0.25 * b.inner_iters + 10, (tt, a.inner_iters, b.inner_iters)
     u32, u64 = per32[-1]["u"], per64[-1]["u"]
     assert np.max(np.abs(u32 - u64)) <= 1e-8 * np.max(np.abs(u64))
