@@ -406,7 +406,8 @@ state 4 density=0.1 energy=0.1 geometry=rectangle xmin=5.0 xmax=6.0 ymin=1.0 yma
 state 5 density=0.1 energy=0.1 geometry=rectangle xmin=5.0 xmax=10.0 ymin=7.0 ymax=8.0
 """
 # algorithmic bytes per interior cell of each timed kernel
-CONFIG2_KERNELS = ((0, "cg_w_step", 48), (1, "cg_ur_step", 48), (4, "cheby_step", 72), (5, "ppcg_inner_sweep", 64))
+CONFIG2_KERNELS = ((0, "cg_w_step", 48), (1, "cg_ur_step", 48), (4, "cheby_step", 72), (5, "ppcg_inner_sweep", 64),
+                   (6, "cheby32_step", 28), (7, "ppcg32_inner_sweep", 32))
 
 
 def config2_deck(n: int, solver: str) -> str:
@@ -454,9 +455,9 @@ def run_config2(args):
         out["solvers"][solver] = {"runs": runs, "ms_per_run": statistics.mean(r["ms"] for r in runs),
                                   "kernels_after_solve": kern}
     # the same decks to the relative true residual 1e-10: FP64 and FP32 inside
-    # FP64 refinement, CG and Chebyshev (one run each)
+    # FP64 refinement, each solver (one run each)
     out["relative"] = {}
-    for solver in [x for x in ("cg", "cheby") if x in chosen]:
+    for solver in [x for x in ("cg", "cheby", "ppcg") if x in chosen]:
         for prec, pname in ((0, "fp64"), (1, "fp32_refined")):
             s = tl.Settings.from_text(config2_deck(n, solver), mode=1, exact=False, criterion=1, precision=prec)
             chunk = tl.initialiseapp(s)

@@ -61,9 +61,9 @@ enum {
   TL_CRIT_REFERENCE = 0,  /* each solver's own test: CG sqrt|rr| < eps (CG.jl:24), others |error| < eps */
   TL_CRIT_RELATIVE = 1    /* sqrt(rr / (u0.u0)) < eps on the recursive residual, then checked on the true one */
 };
-/* TL_PREC_FP32_IR (tealeaf mode, fused kernels): CG, and Chebyshev after its
- * switch, iterate in FP32 inside FP64 refinement to the relative true
- * residual; also in tl_batch_solve (CG). */
+/* TL_PREC_FP32_IR (tealeaf mode, fused kernels): CG, Chebyshev and PPCG
+ * (their CG presteps included) iterate in FP32 inside FP64 refinement to the
+ * relative true residual; also in tl_batch_solve (CG).  Jacobi stays FP64. */
 enum { TL_PREC_FP64 = 0, TL_PREC_FP32_IR = 1 };
 
 /* Chunk(settings) (src/chunk.jl:68-89) */
@@ -196,9 +196,10 @@ int tl_timer_stop(tl_ctx *ctx, double *ms);
 /* Times `reps` back-to-back launches of one fused iteration kernel (0: the CG
  * p-update + stencil + p.w step, 1: the u/r update + r.r step, 2: the FP32
  * stencil step, 3: the FP32 update step, 4: the Chebyshev step, 5: a PPCG
- * inner sweep) on the current fields; for roofline measurements.  The
- * launches overwrite solver work fields (p, w, r, u, sd and their second
- * buffers): call it after the solves whose fields matter. */
+ * inner sweep, 6: the FP32 Chebyshev step, 7: an FP32 PPCG inner sweep) on
+ * the current fields; for roofline measurements.  The launches overwrite
+ * solver work fields (p, w, r, u, sd, their second buffers and the FP32
+ * copies): call it after the solves whose fields matter. */
 int tl_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch);
 
 /* Many independent decks (tealeaf-mode contexts of any sizes on the current

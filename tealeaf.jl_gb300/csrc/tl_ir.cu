@@ -69,6 +69,8 @@ int occupancy32(int kernel, int threads) {
 void tune_w32(tl_ctx *ctx, const Walk &wk) { launch_ir_w(ctx, ctx->ir->p, ctx->ir->pb, 0, &wk); }
 void tune_ur32(tl_ctx *ctx, const Walk &wk) { launch_ir_ur(ctx, ctx->ir->pb, 0, 0, 0, &wk); }
 
+constexpr int NBUF = 9;  // FP32 arrays: kx, ky, p, pb, r, w, x, sd, sdb
+
 int ensure_ir(tl_ctx *ctx) {
   if (ctx->ir) return TL_OK;
   tl_ir_state *ir = new (std::nothrow) tl_ir_state();
@@ -78,16 +80,17 @@ int ensure_ir(tl_ctx *ctx) {
   ir->pitch = (g.X + 31) / 32 * 32;
   ir->lead = (32 - g.hd % 32) % 32;
   ir->stride = (ir->lead + ir->pitch * (long long)g.Y + 64 + 63) / 64 * 64;
-  CK(cudaMalloc(&ir->buf, sizeof(float) * ir->stride * 7));
-  CK(cudaMemsetAsync(ir->buf, 0, sizeof(float) * ir->stride * 7, ctx->stream));
-  float *f[7];
-  for (int k = 0; k < 7; ++k) f[k] = ir->buf + ir->stride * k + ir->lead;
+  CK(cudaMalloc(&ir->buf, sizeof(float) * ir->stride * NBUF));
+  CK(cudaMemsetAsync(ir->buf, 0, sizeof(float) * ir->stride * NBUF, ctx->stream));
+  float *f[NBUF];
+  for (int k = 0; k < NBUF; ++k) f[k] = ir->buf + ir->stride * k + ir->lead;
   ir->kx = f[0]; ir->ky = f[1]; ir->p = f[2]; ir->pb = f[3]; ir->r = f[4]; ir->w = f[5]; ir->x = f[6];
+  ir->sd = f[7]; ir->sdb = f[8];
   // tune on the zeroed buffers, then zero them again: the trial launches
   // leave NaN behind (alpha = 0/0)
   ir->walk_w = tl_autotune(ctx, 128, occupancy32(0, 128), occupancy32(0, 256), tune_w32);
   ir->walk_ur = tl_autotune(ctx, 128, occupancy32(1, 128), occupancy32(1, 256), tune_ur32);
-  CK(cudaMemsetAsync(ir->buf, 0, sizeof(float) * ir->stride * 7, ctx->stream));
+  CK(cudaMemsetAsync(ir->buf, 0, sizeof(float) * ir->stride * NBUF, ctx->stream));
   return TL_OK;
 }
 
@@ -154,12 +157,16 @@ void tl_release_ir_graphs(tl_ctx *ctx) {
       cudaGraphExecDestroy(gx);
       gx = nullptr;
     }
+  for (auto &gx : ctx->ir->ppcg_graph)
+    if (gx) {
+      cudaGraphExecDestroy(gx);
+      gx = nullptr;
+    }
 }
 
 void tl_release_ir(tl_ctx *ctx) {
   if (!ctx->ir) return;
-  for (auto &gx : ctx->ir->graph)
-    if (gx) cudaGraphExecDestroy(gx);
+  tl_release_ir_graphs(ctx);
   if (ctx->ir->buf) cudaFree(ctx->ir->buf);
   delete ctx->ir;
   ctx->ir = nullptr;
@@ -248,6 +255,7 @@ static int ir_loop(tl_ctx *ctx, const tl_params &p, double *rr_out, double *rel_
     rel = bb > 0 ? sqrt(rr / bb) : sqrt(rr);
   }
   float *pcur = which ? ir->pb : ir->p;
+  ir->pwhich = which;
   k_ir_export_p<<<grid_for((long long)ctx->g.nx * ctx->g.ny), 256, 0, ctx->stream>>>(ctx->F, ctx->g, g32, pcur);
   CKL();
   const int up[2] = {TL_EX_U, TL_EX_P};
@@ -295,11 +303,12 @@ int tl_ir_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_resu
 // test (Cheby.jl:25-29) to the inner r.r; when it holds, the correction is
 // folded into u and the true residual measured before the Chebyshev phase
 // takes over.  On return u (with its halo) is the iterate, the host scalars
-// hold the loop's end state, *switched says whether the Chebyshev phase takes
-// over (the switch test held and the true residual is not yet below eps) and
-// *rel_out is the relative true residual.
-int tl_ir_presteps(tl_ctx *ctx, double rx, double ry, const tl_params *prm, int *refinements, double *rel_out,
-                   int *switched) {
+// hold the loop's end state, *switched says whether the Chebyshev (or PPCG)
+// phase takes over (the switch test held and the true residual is not yet
+// below eps), *rr_out is the true r.r and *rel_out its relative value.  The
+// same presteps serve PPCG (PPCG.jl:27-31 is the same test).
+int tl_ir_presteps(tl_ctx *ctx, double rx, double ry, const tl_params *prm, int *refinements, double *rr_out,
+                   double *rel_out, int *switched) {
   int rc = ensure_ir(ctx);
   if (rc) return rc;
   tl_params p = *prm;
@@ -311,28 +320,8 @@ int tl_ir_presteps(tl_ctx *ctx, double rx, double ry, const tl_params *prm, int 
   const int up[2] = {TL_EX_U, TL_EX_P};
   if ((rc = tl_halo_update(ctx, 1, up, 2, 1))) return rc;
   if ((rc = tl_copy_u(ctx))) return rc;
-  double rr = 0.0;
-  if ((rc = ir_loop(ctx, p, &rr, rel_out, refinements))) return rc;
+  if ((rc = ir_loop(ctx, p, rr_out, rel_out, refinements))) return rc;
   *switched = ctx->host_sc->prestep_switch && *rel_out >= p.eps;
-  return TL_OK;
-}
-
-int tl_ir_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch) {
-  int rc = ensure_ir(ctx);
-  if (rc) return rc;
-  if (kernel != 2 && kernel != 3) return TL_ERR_ARG;
-  tl_ir_state *ir = ctx->ir;
-  CK(cudaEventRecord(ctx->tev0, ctx->stream));
-  for (int k = 0; k < reps; ++k) {
-    if (kernel == 2) launch_ir_w(ctx, (k & 1) ? ir->pb : ir->p, (k & 1) ? ir->p : ir->pb, 0);
-    else launch_ir_ur(ctx, ir->pb, 0, 0, 0);
-  }
-  CKL();
-  CK(cudaEventRecord(ctx->tev1, ctx->stream));
-  CK(cudaEventSynchronize(ctx->tev1));
-  float t = 0.f;
-  CK(cudaEventElapsedTime(&t, ctx->tev0, ctx->tev1));
-  *ms_per_launch = t / reps;
   return TL_OK;
 }
 
@@ -565,5 +554,380 @@ int tl_cheby32_run(tl_ctx *ctx, const tl_params *prm, int *refinements, double *
   CKL();
   *refinements = nref;
   *rel_out = rel;
+  return TL_OK;
+}
+
+// ---------------------------------------------------------------------------
+// PPCG in FP32 inside FP64 refinement
+// ---------------------------------------------------------------------------
+
+namespace tl {
+namespace {
+
+// PPCG's update after the W step (PPCG.jl:64-72 with the tealeaf-mode start
+// of the inner sweeps): x += alpha p', r -= alpha w, sd = r / theta.
+struct OpPpcg32UR {
+  static constexpr bool REDUCES = false;
+  Fields F;
+  G32 g;
+  IrPtrs q;
+  const float *__restrict__ p;
+  float *__restrict__ sd;
+  int guard;
+  __device__ bool skip() const { return guard && F.sc->done; }
+  __device__ void on_skip() const {}
+  __device__ void tile(int i0, int j0, int j1, double (&)[1]) const {
+    if (i0 >= g.nx) return;
+    const int ncell = min(4, g.nx - i0);
+    const float alpha = (float)F.sc->alpha, theta = (float)F.sc->theta;
+    for (int j = j0; j < j1; ++j) {
+      const size_t c = g.at(i0, j);
+      if (ncell == 4) {
+        const float4 pv = ld4(p + c), wv = ld4(q.w + c);
+        float4 xv = ld4(q.x + c), rv = ld4(q.r + c);
+        xv.x = fmaf(alpha, pv.x, xv.x); xv.y = fmaf(alpha, pv.y, xv.y);
+        xv.z = fmaf(alpha, pv.z, xv.z); xv.w = fmaf(alpha, pv.w, xv.w);
+        rv.x = fmaf(-alpha, wv.x, rv.x); rv.y = fmaf(-alpha, wv.y, rv.y);
+        rv.z = fmaf(-alpha, wv.z, rv.z); rv.w = fmaf(-alpha, wv.w, rv.w);
+        st4(q.x + c, xv);
+        st4(q.r + c, rv);
+        st4(sd + c, make_float4(rv.x / theta, rv.y / theta, rv.z / theta, rv.w / theta));
+      } else {
+        for (int k = 0; k < ncell; ++k) {
+          q.x[c + k] = fmaf(alpha, p[c + k], q.x[c + k]);
+          const float rv = fmaf(-alpha, q.w[c + k], q.r[c + k]);
+          q.r[c + k] = rv;
+          sd[c + k] = rv / theta;
+        }
+      }
+    }
+  }
+  __device__ void fin(const double *) const {}
+};
+
+// One PPCG inner sweep in FP32 (PPCG.jl:74-88, the halo of sd reflected in
+// the index math): r -= A sd, x += sd, sd' = alpha_pp sd + beta_pp r.  The
+// last sweep of an outer step also sums r.r and runs the outer step's
+// epilogue (beta, the iteration count, the refinement test).
+template <bool LAST>
+struct OpPpcg32Inner {
+  static constexpr bool REDUCES = LAST;
+  Fields F;
+  G32 g;
+  IrPtrs q;  // kx, ky, r, x
+  const float *__restrict__ sdsrc;
+  float *__restrict__ sddst;
+  int pp;  // 1-based inner sweep
+  int guard;
+  cudaGraphConditionalHandle cond;
+  int set_cond;
+  __device__ bool skip() const { return guard && F.sc->done; }
+  __device__ void on_skip() const {
+    if (set_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0u);
+  }
+
+  // The per-row operands other than sd, loaded one row ahead of their use.
+  struct Row {
+    float4 kx, r, x;
+    float sw, se, kxe;  // west edge (lane 0), east edge and its kx (lane 31 or the last column)
+  };
+  __device__ __forceinline__ void load_row(Row &o, int i0, int j, bool valid, bool full, bool inner, int lane) const {
+    if (!valid) return;
+    const size_t c = g.at(i0, j);
+    o.kx = ld4(q.kx + c);
+    o.r = ld4(q.r + c);
+    o.x = ld4(q.x + c);
+    if (lane == 0 && i0 > 0) o.sw = __ldg(sdsrc + c - 1);
+    if (full && (lane == 31 || !inner)) {
+      o.kxe = __ldg(q.kx + c + 4);
+      if (inner) o.se = __ldg(sdsrc + c + 4);
+    }
+  }
+
+  __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
+    const int nx = g.nx, ny = g.ny;
+    const int lane = threadIdx.x & 31;
+    const bool valid = i0 < nx;
+    const int ncell = valid ? min(4, nx - i0) : 0;
+    const bool full = ncell == 4;
+    const bool inner = i0 + 4 < nx;
+    const float ca = (float)F.chebyalpha[pp], cb = (float)F.chebybeta[pp];
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto ld = [&](const float *a, int j) { return valid ? ld4(a + g.at(i0, j)) : z; };
+    float4 sc = ld(sdsrc, j0);
+    float4 ss = j0 > 0 ? ld(sdsrc, j0 - 1) : sc;
+    float4 sn = j0 + 1 < ny ? ld(sdsrc, j0 + 1) : sc;
+    float4 kys = ld(q.ky, j0), kyn = ld(q.ky, j0 + 1);
+    Row cur = {}, nxt = {};
+    load_row(cur, i0, j0, valid, full, inner, lane);
+    for (int j = j0; j < j1; ++j) {
+      // next row's operands, and sd and ky two rows ahead
+      float4 snn = z, kynn = z;
+      if (j + 1 < j1) {
+        load_row(nxt, i0, j + 1, valid, full, inner, lane);
+        if (j + 2 < ny) snn = ld(sdsrc, j + 2);
+        kynn = ld(q.ky, j + 2);
+      }
+      float sw = __shfl_up_sync(FULL, sc.w, 1);
+      float se = __shfl_down_sync(FULL, sc.x, 1);
+      float kxe = __shfl_down_sync(FULL, cur.kx.x, 1);
+      float a = 0.f;
+      if (valid) {
+        if (i0 == 0) sw = sc.x;
+        else if (lane == 0) sw = cur.sw;
+        if (full && (lane == 31 || !inner)) {
+          kxe = cur.kxe;
+          se = inner ? cur.se : sc.w;
+        }
+        float rn[4], xn[4], sdn[4];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          rn[m] = 0.f;
+          xn[m] = 0.f;
+          sdn[m] = 0.f;
+          if (m < ncell) {
+            const float c = comp(sc, m);
+            const float e = (m + 1 < ncell) ? comp(sc, m + 1) : (m == 3 ? se : c);
+            const float wl = (m == 0) ? sw : comp(sc, m - 1);
+            const float k1 = (m == 3) ? kxe : comp(cur.kx, m + 1);
+            float w = c;
+            w = fmaf(k1, c - e, w);
+            w = fmaf(comp(cur.kx, m), c - wl, w);
+            w = fmaf(comp(kyn, m), c - comp(sn, m), w);
+            w = fmaf(comp(kys, m), c - comp(ss, m), w);
+            const float r = comp(cur.r, m) - w;
+            rn[m] = r;
+            xn[m] = comp(cur.x, m) + c;
+            sdn[m] = fmaf(ca, c, cb * r);
+            if (LAST) a = fmaf(r, r, a);
+          }
+        }
+        const size_t c0 = g.at(i0, j);
+        if (full) {
+          st4(q.r + c0, make_float4(rn[0], rn[1], rn[2], rn[3]));
+          st4(q.x + c0, make_float4(xn[0], xn[1], xn[2], xn[3]));
+          st4(sddst + c0, make_float4(sdn[0], sdn[1], sdn[2], sdn[3]));
+        } else {
+          for (int m = 0; m < ncell; ++m) {
+            q.r[c0 + m] = rn[m];
+            q.x[c0 + m] = xn[m];
+            sddst[c0 + m] = sdn[m];
+          }
+        }
+      }
+      if (LAST) acc[0] += (double)a;
+      ss = sc;
+      sc = sn;
+      sn = (j + 2 < ny) ? snn : sc;
+      kys = kyn;
+      kyn = kynn;
+      cur = nxt;
+    }
+  }
+  __device__ void fin(const double *tot) const {
+    if (!LAST) return;
+    DevScalars *sc = F.sc;
+    const double rrn = tot[0];
+    sc->beta = rrn / sc->rro;  // PPCG.jl:89-92
+    sc->rro = rrn;
+    sc->error = rrn;
+    sc->iter += 1;
+    sc->cheby_iters += 1;
+    sc->first = 0;
+    const bool claim = sqrt(rrn / sc->bb) < sc->eps;
+    const bool refine = claim || rrn < sc->delta2 * sc->rr_ref;
+    sc->converged = 0;
+    sc->switched = refine;
+    const int done = refine || sc->iter >= sc->maxiters;
+    sc->done = done;
+    if (set_cond) cudaGraphSetConditional(cond, done ? 0u : 1u);
+  }
+};
+
+void launch_ppcg32_ur(tl_ctx *ctx, const float *p, int guard) {
+  OpPpcg32UR op;
+  op.F = ctx->F;
+  op.g = g32_of(ctx);
+  op.q = ptrs_of(ctx);
+  op.p = p;
+  op.sd = ctx->ir->sd;
+  op.guard = guard;
+  const Walk &wk = ctx->ir->walk_ur;
+  k_walk32<OpPpcg32UR><<<wk.blocks, 32 * wk.warps, 0, ctx->stream>>>(op, wk, ctx->g.ny);
+}
+
+void launch_ppcg32_inner(tl_ctx *ctx, int pp, int last, int guard, cudaGraphConditionalHandle cond, int set_cond) {
+  tl_ir_state *ir = ctx->ir;
+  const float *src = (pp & 1) ? ir->sd : ir->sdb;
+  float *dst = (pp & 1) ? ir->sdb : ir->sd;
+  const Walk &wk = ir->walk_w;
+  if (last) {
+    OpPpcg32Inner<true> op;
+    op.F = ctx->F; op.g = g32_of(ctx); op.q = ptrs_of(ctx); op.sdsrc = src; op.sddst = dst; op.pp = pp;
+    op.guard = guard; op.cond = cond; op.set_cond = set_cond;
+    k_walk32<OpPpcg32Inner<true>><<<wk.blocks, 32 * wk.warps, 0, ctx->stream>>>(op, wk, ctx->g.ny);
+  } else {
+    OpPpcg32Inner<false> op;
+    op.F = ctx->F; op.g = g32_of(ctx); op.q = ptrs_of(ctx); op.sdsrc = src; op.sddst = dst; op.pp = pp;
+    op.guard = guard; op.cond = 0; op.set_cond = 0;
+    k_walk32<OpPpcg32Inner<false>><<<wk.blocks, 32 * wk.warps, 0, ctx->stream>>>(op, wk, ctx->g.ny);
+  }
+}
+
+// One PPCG outer step in FP32: W (p' = beta p + r, w = A p', alpha), the
+// update, and n inner sweeps, the last of which closes the step.  `which`
+// selects the buffer that holds p; the step writes p' into the other one.
+void ppcg32_outer(tl_ctx *ctx, int which, int n, int guard, cudaGraphConditionalHandle cond, int set_cond) {
+  tl_ir_state *ir = ctx->ir;
+  float *a = which ? ir->pb : ir->p, *b = which ? ir->p : ir->pb;
+  launch_ir_w(ctx, a, b, guard);
+  launch_ppcg32_ur(ctx, b, 1);
+  for (int pp = 1; pp <= n; ++pp) launch_ppcg32_inner(ctx, pp, pp == n, 1, cond, pp == n && set_cond);
+}
+
+int ppcg32_graph(tl_ctx *ctx, int which, int n, cudaGraphExec_t *out) {
+  tl_ir_state *ir = ctx->ir;
+  if (ir->ppcg_inner != n) {  // the recorded sweeps depend on the inner step count
+    for (auto &gx : ir->ppcg_graph)
+      if (gx) {
+        cudaGraphExecDestroy(gx);
+        gx = nullptr;
+      }
+    ir->ppcg_inner = n;
+  }
+  if (ir->ppcg_graph[which]) {
+    *out = ir->ppcg_graph[which];
+    return TL_OK;
+  }
+  cudaGraph_t graph = nullptr;
+  CK(cudaGraphCreate(&graph, 0));
+  cudaGraphConditionalHandle h;
+  cudaError_t e = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return tl_cuda_fail(ctx, e, "cudaGraphConditionalHandleCreate", __LINE__);
+  }
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return tl_cuda_fail(ctx, e, "cudaGraphAddNode(while)", __LINE__);
+  }
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  e = cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return tl_cuda_fail(ctx, e, "cudaStreamBeginCaptureToGraph", __LINE__);
+  }
+  // two outer steps per trip, p returning to its buffer
+  ppcg32_outer(ctx, which, n, 0, h, 0);
+  ppcg32_outer(ctx, which ^ 1, n, 1, h, 1);
+  cudaError_t le = cudaGetLastError();
+  cudaGraph_t captured = nullptr;
+  e = cudaStreamEndCapture(ctx->stream, &captured);
+  if (e != cudaSuccess || le != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return tl_cuda_fail(ctx, e != cudaSuccess ? e : le, "capture of the FP32 PPCG loop", __LINE__);
+  }
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return tl_cuda_fail(ctx, e, "cudaGraphInstantiate", __LINE__);
+  ir->ppcg_graph[which] = exec;
+  *out = exec;
+  return TL_OK;
+}
+
+}  // namespace
+}  // namespace tl
+
+// The PPCG iteration after its switch, in FP32 inside FP64 refinement
+// (tealeaf mode).  On entry the FP32-refined CG presteps have ended at the
+// switch (tl_ir_presteps): u holds the iterate, r its true residual in FP64
+// and FP32, the search direction is in the FP32 buffer the presteps left it
+// in, and the device scalars hold theta, beta and the inner coefficients.
+// The outer steps continue the search direction; each refinement folds the
+// correction into u, measures the true residual in FP64 and replaces the
+// FP32 residual with it.  Stops on the relative true residual
+// ||u0 - A u|| / ||u0|| < eps or the iteration budget.
+int tl_ppcg32_run(tl_ctx *ctx, const tl_params *prm, double rr, int *refinements, double *rel_out) {
+  int rc = ensure_ir(ctx);
+  if (rc) return rc;
+  tl_ir_state *ir = ctx->ir;
+  const G32 g32 = g32_of(ctx);
+  const int n = prm->ppcginnersteps;
+  if ((rc = tl_read_scalars(ctx))) return rc;
+  const double bb = ctx->host_sc->bb;
+  double rel = bb > 0 ? sqrt(rr / bb) : sqrt(rr);
+  int which = ir->pwhich, nref = 0;
+  ctx->last_solve_ms = 0.0;
+  while (rel >= prm->eps && ctx->host_sc->iter < prm->maxiters) {
+    k_ir_start<<<1, 1, 0, ctx->stream>>>(ctx->F.sc, rr, IR_DELTA * IR_DELTA);
+    CKL();
+    cudaGraphExec_t exec = nullptr;
+    if (!ctx->host_loop && (rc = ppcg32_graph(ctx, which, n, &exec))) return rc;
+    const int before = ctx->host_sc->iter;
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    if (ctx->host_loop) {
+      for (;;) {
+        for (int k = 0; k < 4; ++k) {
+          ppcg32_outer(ctx, which, n, 1, 0, 0);
+          ppcg32_outer(ctx, which ^ 1, n, 1, 0, 0);
+        }
+        CKL();
+        if ((rc = tl_read_scalars(ctx))) return rc;
+        if (ctx->host_sc->done) break;
+      }
+    } else {
+      CK(cudaGraphLaunch(exec, ctx->stream));
+    }
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    CK(cudaEventSynchronize(ctx->ev1));
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1));
+    ctx->last_solve_ms += t;
+    if ((rc = tl_read_scalars(ctx))) return rc;
+    const int steps = ctx->host_sc->iter - before;
+    ctx->launches += 1 + (2LL + n) * steps;
+    if (steps & 1) which ^= 1;  // the last outer step wrote p into the other buffer
+    if ((rc = refine(ctx, &rr))) return rc;
+    ++nref;
+    rel = bb > 0 ? sqrt(rr / bb) : sqrt(rr);
+  }
+  ir->pwhich = which;
+  k_ir_export_p<<<grid_for((long long)ctx->g.nx * ctx->g.ny), 256, 0, ctx->stream>>>(ctx->F, ctx->g, g32,
+                                                                                      which ? ir->pb : ir->p);
+  CKL();
+  *refinements = nref;
+  *rel_out = rel;
+  return TL_OK;
+}
+
+// Back-to-back launches of one FP32 kernel on the current FP32 fields (ids as
+// in tl_bench_kernel): 2 the CG stencil step, 3 the CG update step, 6 the
+// Chebyshev step, 7 a PPCG inner sweep.
+int tl_ir_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch) {
+  int rc = ensure_ir(ctx);
+  if (rc) return rc;
+  if (kernel != 2 && kernel != 3 && kernel != 6 && kernel != 7) return TL_ERR_ARG;
+  tl_ir_state *ir = ctx->ir;
+  CK(cudaEventRecord(ctx->tev0, ctx->stream));
+  for (int k = 0; k < reps; ++k) {
+    if (kernel == 2) launch_ir_w(ctx, (k & 1) ? ir->pb : ir->p, (k & 1) ? ir->p : ir->pb, 0);
+    else if (kernel == 3) launch_ir_ur(ctx, ir->pb, 0, 0, 0);
+    else if (kernel == 6) launch_cheby32(ctx, (k & 1) ? ir->pb : ir->x, (k & 1) ? ir->x : ir->pb, 0);
+    else launch_ppcg32_inner(ctx, 1 + (k & 1), 0, 0, 0, 0);
+  }
+  CKL();
+  CK(cudaEventRecord(ctx->tev1, ctx->stream));
+  CK(cudaEventSynchronize(ctx->tev1));
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, ctx->tev0, ctx->tev1));
+  *ms_per_launch = t / reps;
   return TL_OK;
 }

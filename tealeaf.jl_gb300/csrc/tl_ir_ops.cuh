@@ -16,8 +16,12 @@ struct tl_ir_state {
   float *buf = nullptr;
   long long pitch = 0, lead = 0, stride = 0;
   float *kx = nullptr, *ky = nullptr, *p = nullptr, *pb = nullptr, *r = nullptr, *w = nullptr, *x = nullptr;
+  float *sd = nullptr, *sdb = nullptr;  // PPCG inner sweeps: the update and its second buffer
   tl::Walk walk_w{}, walk_ur{};  // autotuned layouts of the two FP32 kernels
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // p in the first / second buffer
+  cudaGraphExec_t ppcg_graph[2] = {nullptr, nullptr};
+  int ppcg_inner = -1;  // inner sweeps recorded in ppcg_graph
+  int pwhich = 0;       // after a CG loop: 1 when the search direction is in pb
 };
 
 namespace tl {

@@ -279,9 +279,9 @@ int tl_cheby_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_r
   const int fp32 = prm->precision == TL_PREC_FP32_IR && !exact;
   int rc, pre_ref = 0;
   if (fp32) {
-    double rel = -1.0;
+    double rr = 0.0, rel = -1.0;
     int sw = 0;
-    if ((rc = tl_ir_presteps(ctx, rx, ry, prm, &pre_ref, &rel, &sw))) return rc;
+    if ((rc = tl_ir_presteps(ctx, rx, ry, prm, &pre_ref, &rr, &rel, &sw))) return rc;
     if (!sw) {  // converged or out of iterations during the presteps
       fill_result(ctx, res, ctx->host_sc->iter);
       res->refinements = pre_ref;
@@ -371,14 +371,32 @@ int tl_ppcg_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_re
     tl_set_error(ctx, "ppcginnersteps %d: PPCG needs at least one inner sweep", prm->ppcginnersteps);
     return TL_ERR_ARG;
   }
-  int rc = cg_phase(ctx, rx, ry, prm, exact, 0);
-  if (rc) return rc;
-  const DevScalars sc0 = *ctx->host_sc;
-  if (!sc0.switched) {
-    fill_result(ctx, res, sc0.iter);
-    res->error = prm->maxiters >= 1 ? sc0.error : ERROR_START;
-    return TL_OK;
+  // FP32 inner sweeps inside FP64 refinement, for the presteps and the PPCG
+  // steps (tealeaf mode; exact implies FP64)
+  const int fp32 = prm->precision == TL_PREC_FP32_IR && !exact;
+  int rc, pre_ref = 0;
+  double pre_rr = 0.0;
+  if (fp32) {
+    double rel = -1.0;
+    int sw = 0;
+    if ((rc = tl_ir_presteps(ctx, rx, ry, prm, &pre_ref, &pre_rr, &rel, &sw))) return rc;
+    if (!sw) {  // converged or out of iterations during the presteps
+      fill_result(ctx, res, ctx->host_sc->iter);
+      res->refinements = pre_ref;
+      res->rel_residual = rel;
+      res->converged = rel >= 0 && rel < prm->eps;
+      return TL_OK;
+    }
+  } else {
+    if ((rc = cg_phase(ctx, rx, ry, prm, exact, 0))) return rc;
+    const DevScalars sc0 = *ctx->host_sc;
+    if (!sc0.switched) {
+      fill_result(ctx, res, sc0.iter);
+      res->error = prm->maxiters >= 1 ? sc0.error : ERROR_START;
+      return TL_OK;
+    }
   }
+  const DevScalars sc0 = *ctx->host_sc;
   if (ref) {
     res->iters = sc0.iter + 1;
     res->cg_iters = sc0.iter;
@@ -391,6 +409,25 @@ int tl_ppcg_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_re
   double emin, emax, theta;
   if ((rc = eigenvalues(ctx, cgiters, &emin, &emax))) return rc;  // PPCG.jl:41-42
   if ((rc = cheby_coef(ctx, emin, emax, n, &theta))) return rc;
+  if (fp32) {
+    // the presteps' last refinement measured the true residual, which
+    // init! (PPCG.jl:58-61) would compute here
+    if ((rc = set_phase(ctx, theta, 0, 0, 0, 2, 0, 0.0))) return rc;
+    int nref = 0;
+    double rel = -1.0;
+    if ((rc = tl_ppcg32_run(ctx, prm, pre_rr, &nref, &rel))) return rc;
+    const int up[2] = {TL_EX_U, TL_EX_P};
+    if ((rc = tl_halo_update(ctx, 1, up, 2, 1))) return rc;
+    if ((rc = tl_read_scalars(ctx))) return rc;
+    fill_result(ctx, res, cgiters);
+    res->inner_iters = ctx->host_sc->cheby_iters;
+    res->eigmin = emin;
+    res->eigmax = emax;
+    res->refinements = pre_ref + nref;
+    res->rel_residual = rel;
+    res->converged = rel >= 0 && rel < prm->eps;
+    return TL_OK;
+  }
   // init!: residual!, rro = r.r, halo of p (PPCG.jl:58-61)
   launch_residual(ctx->stream, ctx->F, ctx->g, TL_MODE_TEALEAF);
   launch_norm_r(ctx->stream, ctx->F, ctx->g, ctx->walk_exact);

@@ -85,8 +85,9 @@ int tl_ir_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_resu
 int tl_ensure_ir(tl_ctx *ctx);  // allocates and tunes the FP32 refinement buffers
 // Chebyshev after its first step, in FP32 inside FP64 refinement (tl_ir.cu)
 int tl_cheby32_run(tl_ctx *ctx, const tl_params *prm, int *refinements, double *rel_out);
-int tl_ir_presteps(tl_ctx *ctx, double rx, double ry, const tl_params *prm, int *refinements, double *rel_out,
-                   int *switched);
+int tl_ir_presteps(tl_ctx *ctx, double rx, double ry, const tl_params *prm, int *refinements, double *rr_out,
+                   double *rel_out, int *switched);
+int tl_ppcg32_run(tl_ctx *ctx, const tl_params *prm, double rr, int *refinements, double *rel_out);
 int tl_ir_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch);
 tl::Walk *tl_ir_walk(tl_ctx *ctx, int kernel);  // the FP32 kernels' layouts (kernel 2, 3)
 

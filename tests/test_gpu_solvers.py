@@ -132,3 +132,29 @@ def test_cheby_fp32_refined(tl, built_lib, n, seed, pre):
             assert abs(a.inner_iters - b.inner_iters) <= 0.25 * b.inner_iters + 10, (tt, a.inner_iters, b.inner_iters)
     u32, u64 = per32[-1]["u"], per64[-1]["u"]
     assert np.max(np.abs(u32 - u64)) <= 1e-8 * np.max(np.abs(u64))
+
+
+@pytest.mark.parametrize("n,ny,seed,pre,inner", [(200, 200, 53, 30, 5), (243, 150, 56, 15, 10), (77, 131, 54, 20, 3)])
+def test_ppcg_fp32_refined(tl, built_lib, n, ny, seed, pre, inner):
+    """PPCG in FP32 inside FP64 refinement, the CG presteps included: every
+    step meets the 1e-10 relative true residual, with at least one
+    refinement, and the final u matches FP64 PPCG to 1e-8 of its maximum.
+    The switch falls within a few iterations of FP64's; the outer PPCG step
+    counts agree to 25 % (FP64 tests |r.r| < eps, FP32 the relative true
+    residual after each refinement)."""
+    text = random_deck(n, seed, steps=3, eps=1e-10, ny=ny, solver="ppcg", presteps=pre, ppcg_inner_steps=inner)
+    _, r64, _, per64 = gpu_run(tl, text, TEA, exact=False, steps_fields=True, criterion=1, precision=0)
+    _, r32, _, per32 = gpu_run(tl, text, TEA, exact=False, steps_fields=True, criterion=1, precision=1)
+    for tt, (a, b) in enumerate(zip(r32, r64)):
+        assert a.converged and 0 <= a.rel_residual < 1e-10, (tt, a)
+        assert b.converged
+        assert a.refinements >= 1
+        assert abs(a.cg_iters - b.cg_iters) <= 0.05 * b.cg_iters + 2, (tt, a.cg_iters, b.cg_iters)
+        if a.inner_iters:
+            assert a.cg_iters >= pre
+            assert abs(a.inner_iters - b.inner_iters) <= 0.25 * b.inner_iters + 3, (tt, a.inner_iters, b.inner_iters)
+    assert any(a.inner_iters for a in r32), "the deck must reach the switch"
+    # interior only: FP64 PPCG leaves u's halo from the last CG prestep (its
+    # steps exchange p alone, PPCG.jl:31), the FP32 refinements refresh it
+    u32, u64 = per32[-1]["u"][2:-2, 2:-2], per64[-1]["u"][2:-2, 2:-2]
+    assert np.max(np.abs(u32 - u64)) <= 1e-8 * np.max(np.abs(u64))
