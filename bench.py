@@ -215,12 +215,15 @@ def run_e2e(tl, n, precision, steps, warmup, warm=0):
     return statistics.mean(times), 2 * X * Y * 8, X * Y * 8
 
 
+# FP32 CG iteration: the direction step (read p, r, iw; write p': 16 B) and
+# the update step (read p', iw, x, r; write x, r: 24 B)
+IR_ITER_BYTES = 40
 KERNELS = {"fp64": ((0, "cg_w_step", W_STEP_BYTES), (1, "cg_ur_step", UR_STEP_BYTES)),
-           "fp32_ir": ((2, "ir_w_step", 24), (3, "ir_ur_step", 24))}
+           "fp32_ir": ((8, "ir_dir_step", 16), (9, "ir_update_step", 24))}
 # DRAM bytes (read + write) per interior cell of one launch, from the ncu
 # captures at 4096^2 summarised in profiles/*_4096.md; traffic grows with the
 # cells, so a full launch moves this times n^2.
-TRAFFIC_BYTES_PER_CELL = {"ir_w_step": 381.0e6 / 4096 ** 2, "ir_ur_step": 358.5e6 / 4096 ** 2,
+TRAFFIC_BYTES_PER_CELL = {"ir_dir_step": 247.5e6 / 4096 ** 2, "ir_update_step": 361.1e6 / 4096 ** 2,
                           "cg_w_step": 923.7e6 / 4096 ** 2}
 
 
@@ -340,7 +343,7 @@ def gpu_arm(args):
                               "rel_residual": [r.rel_residual for r in results],
                               "loop_ms": loop_ms, "launches": [r.launches for r in results],
                               "ms_per_iteration": statistics.mean(loop_ms) / statistics.mean(iters),
-                              "algorithmic_gbs_per_iteration": (BYTES_PER_CELL_ITER if name == "fp64" else 48) *
+                              "algorithmic_gbs_per_iteration": (BYTES_PER_CELL_ITER if name == "fp64" else IR_ITER_BYTES) *
                               n * n * statistics.mean(iters) / (statistics.mean(loop_ms) * 1e-3) / 1e9,
                               "warm": [r.warm for r in results], "r0_plain": [r.r0_plain for r in results],
                               "r0_pred": [r.r0_pred for r in results]}

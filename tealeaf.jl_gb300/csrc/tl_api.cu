@@ -385,7 +385,7 @@ extern "C" int tl_timer_stop(tl_ctx *ctx, double *ms) {
 extern "C" int tl_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch) {
   if (!ctx || !ms_per_launch || reps < 1 || ctx->cfg.mode != TL_MODE_TEALEAF) return TL_ERR_ARG;
   const Fields &F = ctx->F;
-  if (kernel == 2 || kernel == 3 || kernel == 6 || kernel == 7) return tl_ir_bench_kernel(ctx, kernel, reps, ms_per_launch);
+  if (kernel == 2 || kernel == 3 || (kernel >= 6 && kernel <= 9)) return tl_ir_bench_kernel(ctx, kernel, reps, ms_per_launch);
   if (kernel < 0 || kernel > 5) return TL_ERR_ARG;
   launch_init_diag(ctx->stream, F, ctx->g);
   CKL();
@@ -415,7 +415,9 @@ static Walk *layout_of(tl_ctx *ctx, int kernel) {
     case 0: return &ctx->walk_w64;
     case 1: return &ctx->walk_ur64;
     case 2:
-    case 3: return tl_ir_walk(ctx, kernel);
+    case 3:
+    case 8:
+    case 9: return tl_ir_walk(ctx, kernel);
     default: return nullptr;
   }
 }

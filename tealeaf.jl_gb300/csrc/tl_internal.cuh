@@ -64,6 +64,7 @@ struct DevScalars {
   int finished;         // the deck's solve is over (converged or out of iterations)
   int refinements;      // FP64 refinement steps taken
   int prestep_switch;   // FP32 CG presteps of Chebyshev: the switch test held (Cheby.jl:25-29)
+  double rxh, ryh;      // FP32 stencil from inverse weights: Kx = rxh (iw_l + iw_c), Ky = ryh (iw_d + iw_c)
 };
 
 // Device pointers of one context, passed to kernels by value.

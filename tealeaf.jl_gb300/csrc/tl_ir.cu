@@ -17,6 +17,7 @@
 // w = p + kx1 (p - pE) + kx0 (p - pW) + ky1 (p - pN) + ky0 (p - pS), which
 // keeps the identity term exact where the large coupling terms cancel.
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 
@@ -59,17 +60,70 @@ void launch_ir_ur(tl_ctx *ctx, const float *p, int guard, cudaGraphConditionalHa
   k_walk32<OpIrUR><<<wk.blocks, 32 * wk.warps, 0, ctx->stream>>>(op, wk, ctx->g.ny);
 }
 
-int occupancy32(int kernel, int threads) {
+template <int AHEAD>
+void launch_ir_dir_t(tl_ctx *ctx, const float *psrc, float *pdst, int guard, const Walk &wk) {
+  OpIrDir<AHEAD> op;
+  op.F = ctx->F;
+  op.g = g32_of(ctx);
+  op.q = ptrs_of(ctx);
+  op.psrc = psrc;
+  op.pdst = pdst;
+  op.guard = guard;
+  k_walk32<OpIrDir<AHEAD>><<<wk.blocks, 32 * wk.warps, 0, ctx->stream>>>(op, wk, ctx->g.ny);
+}
+
+void launch_ir_dir(tl_ctx *ctx, const float *psrc, float *pdst, int guard) {
+  if (ctx->ir->dir_ahead == 1) launch_ir_dir_t<1>(ctx, psrc, pdst, guard, ctx->ir->walk_dir);
+  else launch_ir_dir_t<2>(ctx, psrc, pdst, guard, ctx->ir->walk_dir);
+}
+
+template <int AHEAD>
+void launch_ir_update_t(tl_ctx *ctx, const float *p, int guard, cudaGraphConditionalHandle cond, int set_cond,
+                        const Walk &wk) {
+  OpIrUpdate<AHEAD> op;
+  op.F = ctx->F;
+  op.g = g32_of(ctx);
+  op.q = ptrs_of(ctx);
+  op.p = p;
+  op.guard = guard;
+  op.cond = cond;
+  op.set_cond = set_cond;
+  k_walk32<OpIrUpdate<AHEAD>><<<wk.blocks, 32 * wk.warps, 0, ctx->stream>>>(op, wk, ctx->g.ny);
+}
+
+void launch_ir_update(tl_ctx *ctx, const float *p, int guard, cudaGraphConditionalHandle cond, int set_cond) {
+  if (ctx->ir->upd_ahead == 1) launch_ir_update_t<1>(ctx, p, guard, cond, set_cond, ctx->ir->walk_upd);
+  else launch_ir_update_t<2>(ctx, p, guard, cond, set_cond, ctx->ir->walk_upd);
+}
+
+template <class Op>
+int occupancy_of(int threads) {
   int n = 0;
-  cudaError_t e = kernel == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_walk32<OpIrW>, threads, 0)
-                              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_walk32<OpIrUR>, threads, 0);
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_walk32<Op>, threads, 0);
   return e == cudaSuccess ? n : 1;
 }
 
 void tune_w32(tl_ctx *ctx, const Walk &wk) { launch_ir_w(ctx, ctx->ir->p, ctx->ir->pb, 0, &wk); }
 void tune_ur32(tl_ctx *ctx, const Walk &wk) { launch_ir_ur(ctx, ctx->ir->pb, 0, 0, 0, &wk); }
+void tune_dir2(tl_ctx *ctx, const Walk &wk) { launch_ir_dir_t<2>(ctx, ctx->ir->p, ctx->ir->pb, 0, wk); }
+void tune_dir1(tl_ctx *ctx, const Walk &wk) { launch_ir_dir_t<1>(ctx, ctx->ir->p, ctx->ir->pb, 0, wk); }
+void tune_upd2(tl_ctx *ctx, const Walk &wk) { launch_ir_update_t<2>(ctx, ctx->ir->pb, 0, 0, 0, wk); }
+void tune_upd1(tl_ctx *ctx, const Walk &wk) { launch_ir_update_t<1>(ctx, ctx->ir->pb, 0, 0, 0, wk); }
 
-constexpr int NBUF = 9;  // FP32 arrays: kx, ky, p, pb, r, w, x, sd, sdb
+// Average time of `reps` launches of one tuned form (after two warm-up launches).
+float time_form(tl_ctx *ctx, void (*launch)(tl_ctx *, const Walk &), const Walk &wk, int reps) {
+  launch(ctx, wk);
+  launch(ctx, wk);
+  float ms = -1.f;
+  if (cudaEventRecord(ctx->tev0, ctx->stream) != cudaSuccess) return ms;
+  for (int k = 0; k < reps; ++k) launch(ctx, wk);
+  if (cudaEventRecord(ctx->tev1, ctx->stream) != cudaSuccess || cudaEventSynchronize(ctx->tev1) != cudaSuccess)
+    return ms;
+  cudaEventElapsedTime(&ms, ctx->tev0, ctx->tev1);
+  return ms / reps;
+}
+
+constexpr int NBUF = 10;  // FP32 arrays: kx, ky, p, pb, r, w, x, sd, sdb, iw
 
 int ensure_ir(tl_ctx *ctx) {
   if (ctx->ir) return TL_OK;
@@ -85,11 +139,29 @@ int ensure_ir(tl_ctx *ctx) {
   float *f[NBUF];
   for (int k = 0; k < NBUF; ++k) f[k] = ir->buf + ir->stride * k + ir->lead;
   ir->kx = f[0]; ir->ky = f[1]; ir->p = f[2]; ir->pb = f[3]; ir->r = f[4]; ir->w = f[5]; ir->x = f[6];
-  ir->sd = f[7]; ir->sdb = f[8];
+  ir->sd = f[7]; ir->sdb = f[8]; ir->iw = f[9];
   // tune on the zeroed buffers, then zero them again: the trial launches
   // leave NaN behind (alpha = 0/0)
-  ir->walk_w = tl_autotune(ctx, 128, occupancy32(0, 128), occupancy32(0, 256), tune_w32);
-  ir->walk_ur = tl_autotune(ctx, 128, occupancy32(1, 128), occupancy32(1, 256), tune_ur32);
+  ir->walk_w = tl_autotune(ctx, 128, occupancy_of<OpIrW>(128), occupancy_of<OpIrW>(256), tune_w32);
+  ir->walk_ur = tl_autotune(ctx, 128, occupancy_of<OpIrUR>(128), occupancy_of<OpIrUR>(256), tune_ur32);
+  // OpIrDir, OpIrUpdate: each form tuned, then the faster one kept (without
+  // tuning, TEALEAF_GB300_TUNE=0: the fixed layout and the two-row-ahead
+  // direction step with the as-reached update step)
+  const char *tune = getenv("TEALEAF_GB300_TUNE");
+  const bool tuning = !(tune && !strcmp(tune, "0"));
+  const Walk d2 = tl_autotune(ctx, 128, occupancy_of<OpIrDir<2>>(128), occupancy_of<OpIrDir<2>>(256), tune_dir2);
+  const Walk d1 = tl_autotune(ctx, 128, occupancy_of<OpIrDir<1>>(128), occupancy_of<OpIrDir<1>>(256), tune_dir1);
+  const float s2 = tuning ? time_form(ctx, tune_dir2, d2, 5) : 0.f;
+  const float s1 = tuning ? time_form(ctx, tune_dir1, d1, 5) : 1.f;
+  ir->dir_ahead = (s1 >= 0.f && s2 >= 0.f && s1 < s2) ? 1 : 2;
+  ir->walk_dir = ir->dir_ahead == 1 ? d1 : d2;
+  const Walk u2 = tl_autotune(ctx, 128, occupancy_of<OpIrUpdate<2>>(128), occupancy_of<OpIrUpdate<2>>(256), tune_upd2);
+  const Walk u1 = tl_autotune(ctx, 128, occupancy_of<OpIrUpdate<1>>(128), occupancy_of<OpIrUpdate<1>>(256), tune_upd1);
+  const float t2 = tuning ? time_form(ctx, tune_upd2, u2, 5) : 1.f;
+  const float t1 = tuning ? time_form(ctx, tune_upd1, u1, 5) : 0.f;
+  ir->upd_ahead = (t1 >= 0.f && t2 >= 0.f && t1 < t2) ? 1 : 2;
+  ir->walk_upd = ir->upd_ahead == 1 ? u1 : u2;
+  cudaGetLastError();
   CK(cudaMemsetAsync(ir->buf, 0, sizeof(float) * ir->stride * NBUF, ctx->stream));
   return TL_OK;
 }
@@ -126,10 +198,10 @@ int ir_graph(tl_ctx *ctx, int which, cudaGraphExec_t *out) {
     return tl_cuda_fail(ctx, e, "cudaStreamBeginCaptureToGraph", __LINE__);
   }
   float *a = which ? ir->pb : ir->p, *b = which ? ir->p : ir->pb;
-  launch_ir_w(ctx, a, b, 0);
-  launch_ir_ur(ctx, b, 0, h, 0);
-  launch_ir_w(ctx, b, a, 1);
-  launch_ir_ur(ctx, a, 1, h, 1);
+  launch_ir_dir(ctx, a, b, 0);
+  launch_ir_update(ctx, b, 0, h, 0);
+  launch_ir_dir(ctx, b, a, 1);
+  launch_ir_update(ctx, a, 1, h, 1);
   cudaError_t le = cudaGetLastError();
   cudaGraph_t captured = nullptr;
   e = cudaStreamEndCapture(ctx->stream, &captured);
@@ -202,13 +274,16 @@ static int refine(tl_ctx *ctx, double *rr, float *e = nullptr) {
 // residual is below eps, the iteration budget is spent or, as CG presteps of
 // Chebyshev (switch rule 1), the switch test held; the FP32 search direction
 // is exported into p.  Returns the last true r.r and its relative value.
-static int ir_loop(tl_ctx *ctx, const tl_params &p, double *rr_out, double *rel_out, int *refinements) {
+static int ir_loop(tl_ctx *ctx, const tl_params &p, double rx, double ry, double *rr_out, double *rel_out,
+                   int *refinements) {
   const G32 g32 = g32_of(ctx);
   tl_ir_state *ir = ctx->ir;
   k_ir_convert<<<grid_for((long long)ctx->g.X * ctx->g.Y), 256, 0, ctx->stream>>>(ctx->F, ctx->g, g32, ir->kx, ir->ky,
                                                                                   ir->r, ir->p, ir->x);
+  k_ir_convert_iw<<<grid_for((long long)ctx->g.X * ctx->g.Y), 256, 0, ctx->stream>>>(ctx->F, ctx->g, g32, ir->iw,
+                                                                                     p.coefficient, rx, ry);
   CKL();
-  ctx->launches += 8;
+  ctx->launches += 9;
   int rc = tl_read_scalars(ctx);
   if (rc) return rc;
   const double bb = ctx->host_sc->bb;
@@ -228,10 +303,10 @@ static int ir_loop(tl_ctx *ctx, const tl_params &p, double *rr_out, double *rel_
       float *a = which ? ir->pb : ir->p, *b = which ? ir->p : ir->pb;
       for (;;) {
         for (int k = 0; k < 8; ++k) {
-          launch_ir_w(ctx, a, b, 1);
-          launch_ir_ur(ctx, b, 1, 0, 0);
-          launch_ir_w(ctx, b, a, 1);
-          launch_ir_ur(ctx, a, 1, 0, 0);
+          launch_ir_dir(ctx, a, b, 1);
+          launch_ir_update(ctx, b, 1, 0, 0);
+          launch_ir_dir(ctx, b, a, 1);
+          launch_ir_update(ctx, a, 1, 0, 0);
         }
         CKL();
         if ((rc = tl_read_scalars(ctx))) return rc;
@@ -285,7 +360,7 @@ int tl_ir_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_resu
   if (prm->warmstart && (rc = tl_warm_try(ctx, rx, ry, prm->warmstart, res))) return rc;
   double rr = 0.0, rel = 0.0;
   int refinements = 0;
-  if ((rc = ir_loop(ctx, p, &rr, &rel, &refinements))) return rc;
+  if ((rc = ir_loop(ctx, p, rx, ry, &rr, &rel, &refinements))) return rc;
   res->iters = ctx->host_sc->iter;
   res->cg_iters = ctx->host_sc->iter;
   res->error = rr;
@@ -320,14 +395,20 @@ int tl_ir_presteps(tl_ctx *ctx, double rx, double ry, const tl_params *prm, int 
   const int up[2] = {TL_EX_U, TL_EX_P};
   if ((rc = tl_halo_update(ctx, 1, up, 2, 1))) return rc;
   if ((rc = tl_copy_u(ctx))) return rc;
-  if ((rc = ir_loop(ctx, p, rr_out, rel_out, refinements))) return rc;
+  if ((rc = ir_loop(ctx, p, rx, ry, rr_out, rel_out, refinements))) return rc;
   *switched = ctx->host_sc->prestep_switch && *rel_out >= p.eps;
   return TL_OK;
 }
 
 tl::Walk *tl_ir_walk(tl_ctx *ctx, int kernel) {
   if (ensure_ir(ctx)) return nullptr;
-  return kernel == 2 ? &ctx->ir->walk_w : &ctx->ir->walk_ur;
+  switch (kernel) {
+    case 2: return &ctx->ir->walk_w;
+    case 3: return &ctx->ir->walk_ur;
+    case 8: return &ctx->ir->walk_dir;
+    case 9: return &ctx->ir->walk_upd;
+    default: return nullptr;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -909,17 +990,19 @@ int tl_ppcg32_run(tl_ctx *ctx, const tl_params *prm, double rr, int *refinements
 }
 
 // Back-to-back launches of one FP32 kernel on the current FP32 fields (ids as
-// in tl_bench_kernel): 2 the CG stencil step, 3 the CG update step, 6 the
-// Chebyshev step, 7 a PPCG inner sweep.
+// in tl_bench_kernel): 2 OpIrW, 3 OpIrUR, 6 the Chebyshev step, 7 a PPCG
+// inner sweep, 8 OpIrDir, 9 OpIrUpdate.
 int tl_ir_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch) {
   int rc = ensure_ir(ctx);
   if (rc) return rc;
-  if (kernel != 2 && kernel != 3 && kernel != 6 && kernel != 7) return TL_ERR_ARG;
+  if (kernel != 2 && kernel != 3 && (kernel < 6 || kernel > 9)) return TL_ERR_ARG;
   tl_ir_state *ir = ctx->ir;
   CK(cudaEventRecord(ctx->tev0, ctx->stream));
   for (int k = 0; k < reps; ++k) {
     if (kernel == 2) launch_ir_w(ctx, (k & 1) ? ir->pb : ir->p, (k & 1) ? ir->p : ir->pb, 0);
     else if (kernel == 3) launch_ir_ur(ctx, ir->pb, 0, 0, 0);
+    else if (kernel == 8) launch_ir_dir(ctx, (k & 1) ? ir->pb : ir->p, (k & 1) ? ir->p : ir->pb, 0);
+    else if (kernel == 9) launch_ir_update(ctx, ir->pb, 0, 0, 0);
     else if (kernel == 6) launch_cheby32(ctx, (k & 1) ? ir->pb : ir->x, (k & 1) ? ir->x : ir->pb, 0);
     else launch_ppcg32_inner(ctx, 1 + (k & 1), 0, 0, 0, 0);
   }

@@ -17,7 +17,10 @@ struct tl_ir_state {
   long long pitch = 0, lead = 0, stride = 0;
   float *kx = nullptr, *ky = nullptr, *p = nullptr, *pb = nullptr, *r = nullptr, *w = nullptr, *x = nullptr;
   float *sd = nullptr, *sdb = nullptr;  // PPCG inner sweeps: the update and its second buffer
-  tl::Walk walk_w{}, walk_ur{};  // autotuned layouts of the two FP32 kernels
+  float *iw = nullptr;                  // 1 / w (w = rho or 1/rho, CG.jl:57-60), halo included
+  tl::Walk walk_w{}, walk_ur{};    // autotuned layouts of OpIrW, OpIrUR (and the Chebyshev/PPCG sweeps)
+  tl::Walk walk_dir{}, walk_upd{};  // autotuned layouts of OpIrDir, OpIrUpdate (the CG iteration)
+  int upd_ahead = 2, dir_ahead = 2;  // the faster OpIrUpdate / OpIrDir form after tuning (its AHEAD)
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // p in the first / second buffer
   cudaGraphExec_t ppcg_graph[2] = {nullptr, nullptr};
   int ppcg_inner = -1;  // inner sweeps recorded in ppcg_graph
@@ -39,6 +42,7 @@ struct G32 {
 
 struct IrPtrs {
   float *kx, *ky, *r, *w, *x;
+  float *iw;  // inverse weights (the CG step pair OpIrDir / OpIrUpdate)
 };
 
 __device__ __forceinline__ float4 ld4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
@@ -204,6 +208,35 @@ struct OpIrW {
   }
 };
 
+// The epilogue of an FP32 CG step (OpIrUR, OpIrUpdate): beta, the iteration
+// count, the refinement test and, as CG presteps of Chebyshev or PPCG, the
+// coefficient table and the switch test.
+__device__ __forceinline__ void ir_cg_epilogue(const Fields &F, double rrn, cudaGraphConditionalHandle cond,
+                                             int set_cond) {
+  DevScalars *sc = F.sc;
+  sc->beta = rrn / sc->rro;
+  bool sw = false;
+  if (sc->switch_rule == 1) {
+    // CG presteps of Chebyshev: the beta table and the switch test
+    // (Cheby.jl:25-29) on this step's r.r
+    if (sc->iter < sc->maxiters) F.cgbeta[sc->iter + 1] = sc->beta;
+    const int tt = sc->iter + 2;  // the solver loop's next trip
+    sw = sc->errorswitch ? (rrn < sc->epslim && tt > CGEIGENITERS) : (tt > sc->presteps && rrn < ERROR_SWITCH_MAX);
+  }
+  sc->rro = rrn;
+  sc->error = rrn;
+  sc->iter += 1;
+  sc->first = 0;
+  const bool claim = sqrt(rrn / sc->bb) < sc->eps;
+  const bool refine = claim || rrn < sc->delta2 * sc->rr_ref;
+  sc->converged = 0;
+  sc->switched = refine;
+  sc->prestep_switch = sw;
+  const int done = refine || sw || sc->iter >= sc->maxiters;
+  sc->done = done;
+  if (set_cond) cudaGraphSetConditional(cond, done ? 0u : 1u);
+}
+
 // UR step: x += alpha p', r -= alpha w, r.r; the epilogue decides whether the
 // next step is another FP32 iteration or a refinement.
 struct OpIrUR {
@@ -248,31 +281,283 @@ struct OpIrUR {
     }
     acc[0] = a;
   }
+  __device__ void fin(const double *tot) const { ir_cg_epilogue(F, tot[0], cond, set_cond); }
+};
+
+
+// ---- the 40-byte CG step pair ----------------------------------------------
+// OpIrDir forms p' = beta p + r and p'.A p' and stores p' (reads p, r, iw:
+// 16 B per cell with the store); OpIrUpdate recomputes w = A p' from the
+// stored p' and does x += alpha p', r -= alpha w, r.r (reads p', iw, x, r,
+// writes x, r: 24 B).  Against OpIrW + OpIrUR (48 B) neither w nor Kx, Ky is
+// stored: the faces come from the inverse weights, Kx = rx/2 (iw_l + iw_c).
+// Both kernels evaluate the stencil with the same function on the same
+// floats, so the w of the update equals the w of the dot bit for bit.
+
+// The five-point neighbourhood of a lane's four cells, after the reflective
+// boundary has been applied (west/east: the edge values beyond the lane's
+// cells; s/n: the rows below and above).
+struct Hood4 {
+  float4 c, s, n;
+  float w, e;
+};
+
+__device__ __forceinline__ void stencil4(const Hood4 &p, const Hood4 &iw, float rxh, float ryh, int ncell,
+                                         float (&out)[4]) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    out[k] = 0.f;
+    if (k < ncell) {
+      const float c = comp(p.c, k), ic = comp(iw.c, k);
+      const bool last = k + 1 == ncell;
+      const float e = last ? (k == 3 ? p.e : c) : comp(p.c, k + 1);
+      const float ie = last ? (k == 3 ? iw.e : ic) : comp(iw.c, k + 1);
+      const float wl = k == 0 ? p.w : comp(p.c, k - 1);
+      const float il = k == 0 ? iw.w : comp(iw.c, k - 1);
+      float t = c;
+      t = fmaf(rxh * (ic + ie), c - e, t);
+      t = fmaf(rxh * (ic + il), c - wl, t);
+      t = fmaf(ryh * (ic + comp(iw.n, k)), c - comp(p.n, k), t);
+      t = fmaf(ryh * (ic + comp(iw.s, k)), c - comp(p.s, k), t);
+      out[k] = t;
+    }
+  }
+}
+
+// The west/east edge values of a lane's four cells from a row's float4s:
+// neighbours by shuffle, lane 0 / lane 31 from their own edge loads, and the
+// reflection at the domain boundary (the cell itself).
+__device__ __forceinline__ void edges4(float4 v, float wload, float eload, int i0, int lane, bool full, bool inner,
+                                       float &w, float &e) {
+  w = __shfl_up_sync(FULL, v.w, 1);
+  e = __shfl_down_sync(FULL, v.x, 1);
+  if (i0 == 0) w = v.x;
+  else if (lane == 0) w = wload;
+  if (full) {
+    if (!inner) e = v.w;
+    else if (lane == 31) e = eload;
+  }
+}
+
+// p' = beta p + r (p on the first step), p'.A p'; stores p'.  AHEAD: rows
+// loaded two rows ahead of their use (2) or as they are reached (1).
+template <int AHEAD>
+struct OpIrDir {
+  static constexpr bool REDUCES = true;
+  Fields F;
+  G32 g;
+  IrPtrs q;
+  const float *__restrict__ psrc;
+  float *__restrict__ pdst;
+  int guard;
+  __device__ bool skip() const { return guard && F.sc->done; }
+  __device__ void on_skip() const {}
+
+  struct Row {
+    float4 p, r, iw;
+    float pw, rw, pe, re, iww, iwe;  // edge loads (lane 0: i0-1, lane 31: i0+4)
+  };
+  __device__ __forceinline__ void load_row(Row &o, int i0, int j, bool valid, bool first, int lane,
+                                           bool inner) const {
+    if (!valid) return;
+    const size_t c = g.at(i0, j);
+    o.p = ld4(psrc + c);
+    o.iw = ld4(q.iw + c);
+    if (!first) o.r = ld4(q.r + c);
+    if (lane == 0 && i0 > 0) {
+      o.pw = __ldg(psrc + c - 1);
+      o.iww = __ldg(q.iw + c - 1);
+      if (!first) o.rw = __ldg(q.r + c - 1);
+    }
+    if (lane == 31 && inner) {
+      o.pe = __ldg(psrc + c + 4);
+      o.iwe = __ldg(q.iw + c + 4);
+      if (!first) o.re = __ldg(q.r + c + 4);
+    }
+  }
+
+  __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
+    const int nx = g.nx, ny = g.ny;
+    const int lane = threadIdx.x & 31;
+    const bool valid = i0 < nx;
+    const int ncell = valid ? min(4, nx - i0) : 0;
+    const bool full = ncell == 4;
+    const bool inner = i0 + 4 < nx;
+    const float beta = (float)F.sc->beta;
+    const float rxh = (float)F.sc->rxh, ryh = (float)F.sc->ryh;
+    const bool first = F.sc->first != 0;
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto pnew = [&](const Row &o) {
+      return first ? o.p
+                   : make_float4(fmaf(beta, o.p.x, o.r.x), fmaf(beta, o.p.y, o.r.y), fmaf(beta, o.p.z, o.r.z),
+                                 fmaf(beta, o.p.w, o.r.w));
+    };
+    Row cur = {}, nxt = {}, sth = {};
+    load_row(cur, i0, j0, valid, first, lane, inner);
+    if (j0 > 0) load_row(sth, i0, j0 - 1, valid, first, -1, inner);
+    if (AHEAD == 2 && j0 + 1 < ny) load_row(nxt, i0, j0 + 1, valid, first, lane, inner);
+    float4 pc = valid ? pnew(cur) : z;
+    float4 ps = (j0 > 0 && valid) ? pnew(sth) : pc;
+    float4 is = (j0 > 0 && valid) ? sth.iw : cur.iw;
+    for (int j = j0; j < j1; ++j) {
+      Row nn = {};
+      if (AHEAD == 2) {
+        if (j + 1 < j1 && j + 2 < ny) load_row(nn, i0, j + 2, valid, first, lane, inner);
+      } else if (j + 1 < ny) {
+        load_row(nxt, i0, j + 1, valid, first, lane, inner);
+      }
+      const bool has_n = j + 1 < ny;
+      const float4 pn = (has_n && valid) ? pnew(nxt) : pc;
+      const float4 in = has_n ? nxt.iw : cur.iw;
+      Hood4 hp, hi;
+      hp.c = pc; hp.s = ps; hp.n = pn;
+      hi.c = cur.iw; hi.s = is; hi.n = in;
+      const float pwl = first ? cur.pw : fmaf(beta, cur.pw, cur.rw);
+      const float pel = first ? cur.pe : fmaf(beta, cur.pe, cur.re);
+      edges4(pc, pwl, pel, i0, lane, full, inner, hp.w, hp.e);
+      edges4(cur.iw, cur.iww, cur.iwe, i0, lane, full, inner, hi.w, hi.e);
+      if (valid) {
+        float wv[4];
+        stencil4(hp, hi, rxh, ryh, ncell, wv);
+        float part = 0.f;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (k < ncell) part = fmaf(wv[k], comp(pc, k), part);
+        acc[0] += (double)part;
+        const size_t c0 = g.at(i0, j);
+        if (full) {
+          st4(pdst + c0, pc);
+        } else {
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            if (k < ncell) pdst[c0 + k] = comp(pc, k);
+        }
+      }
+      ps = pc;
+      pc = pn;
+      is = cur.iw;
+      cur = nxt;
+      if (AHEAD == 2) nxt = nn;
+    }
+  }
   __device__ void fin(const double *tot) const {
     DevScalars *sc = F.sc;
-    const double rrn = tot[0];
-    sc->beta = rrn / sc->rro;
-    bool sw = false;
-    if (sc->switch_rule == 1) {
-      // CG presteps of Chebyshev: the beta table and the switch test
-      // (Cheby.jl:25-29) on this step's r.r
-      if (sc->iter < sc->maxiters) F.cgbeta[sc->iter + 1] = sc->beta;
-      const int tt = sc->iter + 2;  // the solver loop's next trip
-      sw = sc->errorswitch ? (rrn < sc->epslim && tt > CGEIGENITERS) : (tt > sc->presteps && rrn < ERROR_SWITCH_MAX);
-    }
-    sc->rro = rrn;
-    sc->error = rrn;
-    sc->iter += 1;
-    sc->first = 0;
-    const bool claim = sqrt(rrn / sc->bb) < sc->eps;
-    const bool refine = claim || rrn < sc->delta2 * sc->rr_ref;
-    sc->converged = 0;
-    sc->switched = refine;
-    sc->prestep_switch = sw;
-    const int done = refine || sw || sc->iter >= sc->maxiters;
-    sc->done = done;
-    if (set_cond) cudaGraphSetConditional(cond, done ? 0u : 1u);
+    sc->pw = tot[0];
+    sc->alpha = sc->rro / sc->pw;
+    if (sc->switch_rule == 1 && sc->iter < sc->maxiters) F.cgalpha[sc->iter + 1] = sc->alpha;
   }
+};
+
+// w = A p' (recomputed from the stored p'), x += alpha p', r -= alpha w, r.r;
+// the epilogue is OpIrUR's (the refinement test, the Chebyshev switch test
+// as presteps).  AHEAD: the stencil rows are loaded two rows ahead of their
+// use (2) or as the row is reached (1, fewer registers and more resident
+// warps); x and r are loaded one row ahead in both.
+template <int AHEAD>
+struct OpIrUpdate {
+  static constexpr bool REDUCES = true;
+  Fields F;
+  G32 g;
+  IrPtrs q;
+  const float *__restrict__ p;
+  int guard;
+  cudaGraphConditionalHandle cond;
+  int set_cond;
+  __device__ bool skip() const { return guard && F.sc->done; }
+  __device__ void on_skip() const {
+    if (set_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0u);
+  }
+
+  struct Nb {  // the stencil operands of one row
+    float4 p, iw;
+    float pw, pe, iww, iwe;
+  };
+  __device__ __forceinline__ void load_nb(Nb &o, int i0, int j, bool valid, int lane, bool inner) const {
+    if (!valid) return;
+    const size_t c = g.at(i0, j);
+    o.p = ld4(p + c);
+    o.iw = ld4(q.iw + c);
+    if (lane == 0 && i0 > 0) {
+      o.pw = __ldg(p + c - 1);
+      o.iww = __ldg(q.iw + c - 1);
+    }
+    if (lane == 31 && inner) {
+      o.pe = __ldg(p + c + 4);
+      o.iwe = __ldg(q.iw + c + 4);
+    }
+  }
+
+  __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
+    const int nx = g.nx, ny = g.ny;
+    const int lane = threadIdx.x & 31;
+    const bool valid = i0 < nx;
+    const int ncell = valid ? min(4, nx - i0) : 0;
+    const bool full = ncell == 4;
+    const bool inner = i0 + 4 < nx;
+    const float alpha = (float)F.sc->alpha;
+    const float rxh = (float)F.sc->rxh, ryh = (float)F.sc->ryh;
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto ld = [&](const float *a, int j) { return valid ? ld4(a + g.at(i0, j)) : z; };
+    Nb cur = {}, nxt = {};
+    load_nb(cur, i0, j0, valid, lane, inner);
+    float4 xc = ld(q.x, j0), rc = ld(q.r, j0);
+    float4 ps = (j0 > 0 && valid) ? ld(p, j0 - 1) : cur.p;
+    float4 is = (j0 > 0 && valid) ? ld(q.iw, j0 - 1) : cur.iw;
+    if (AHEAD == 2 && j0 + 1 < ny) load_nb(nxt, i0, j0 + 1, valid, lane, inner);
+    double a = acc[0];
+    for (int j = j0; j < j1; ++j) {
+      Nb nn = {};
+      if (AHEAD == 2) {
+        if (j + 1 < j1 && j + 2 < ny) load_nb(nn, i0, j + 2, valid, lane, inner);
+      } else if (j + 1 < ny) {
+        load_nb(nxt, i0, j + 1, valid, lane, inner);
+      }
+      float4 xn = z, rn = z;
+      if (j + 1 < j1) {
+        xn = ld(q.x, j + 1);
+        rn = ld(q.r, j + 1);
+      }
+      const bool has_n = j + 1 < ny;
+      Hood4 hp, hi;
+      hp.c = cur.p; hp.s = ps; hp.n = has_n ? nxt.p : cur.p;
+      hi.c = cur.iw; hi.s = is; hi.n = has_n ? nxt.iw : cur.iw;
+      edges4(cur.p, cur.pw, cur.pe, i0, lane, full, inner, hp.w, hp.e);
+      edges4(cur.iw, cur.iww, cur.iwe, i0, lane, full, inner, hi.w, hi.e);
+      if (valid) {
+        float wv[4];
+        stencil4(hp, hi, rxh, ryh, ncell, wv);
+        float xv[4], rv[4];
+        float part = 0.f;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          xv[k] = fmaf(alpha, comp(cur.p, k), comp(xc, k));
+          rv[k] = fmaf(-alpha, wv[k], comp(rc, k));
+          if (k < ncell) part = fmaf(rv[k], rv[k], part);
+        }
+        a += (double)part;
+        const size_t c0 = g.at(i0, j);
+        if (full) {
+          st4(q.x + c0, make_float4(xv[0], xv[1], xv[2], xv[3]));
+          st4(q.r + c0, make_float4(rv[0], rv[1], rv[2], rv[3]));
+        } else {
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            if (k < ncell) {
+              q.x[c0 + k] = xv[k];
+              q.r[c0 + k] = rv[k];
+            }
+        }
+      }
+      ps = cur.p;
+      is = cur.iw;
+      cur = nxt;
+      if (AHEAD == 2) nxt = nn;
+      xc = xn;
+      rc = rn;
+    }
+    acc[0] = a;
+  }
+  __device__ void fin(const double *tot) const { ir_cg_epilogue(F, tot[0], cond, set_cond); }
 };
 
 // Refinement: u += x, x = 0 on the interior.
@@ -332,6 +617,23 @@ __global__ void k_ir_convert(Fields F, Geom g, G32 g32, float *kx, float *ky, fl
   }
 }
 
+// The FP32 inverse weights iw = 1/w over the whole array (w = rho for
+// conductivity, 1/rho for its reciprocal: CG.jl:57-60 over the whole array,
+// the tealeaf-mode range) and the face factors rx/2, ry/2, so that
+// Kx = rx (w_l + w_c) / (2 w_l w_c) = rx/2 (iw_l + iw_c) (CG.jl:62-67).
+__global__ void k_ir_convert_iw(Fields F, Geom g, G32 g32, float *iw, int coefficient, double rx, double ry) {
+  const long long n = (long long)g.X * g.Y;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    F.sc->rxh = 0.5 * rx;
+    F.sc->ryh = 0.5 * ry;
+  }
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const int I = (int)(k % g.X), J = (int)(k / g.X);
+    const double rho = F.density[(size_t)I + (size_t)J * g.pitch];
+    iw[(size_t)I + (size_t)J * g32.pitch] = (float)(coefficient == TL_CONDUCTIVITY ? 1.0 / rho : rho);
+  }
+}
+
 // p (FP64) = (double) p32 on the interior: the last search direction.
 __global__ void k_ir_export_p(Fields F, Geom g, G32 g32, const float *p32) {
   const long long n = (long long)g.nx * g.ny;
@@ -368,6 +670,7 @@ IrPtrs ptrs_of(tl_ctx *ctx) {
   q.r = ctx->ir->r;
   q.w = ctx->ir->w;
   q.x = ctx->ir->x;
+  q.iw = ctx->ir->iw;
   return q;
 }
 
