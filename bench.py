@@ -410,7 +410,7 @@ state 5 density=0.1 energy=0.1 geometry=rectangle xmin=5.0 xmax=10.0 ymin=7.0 ym
 """
 # algorithmic bytes per interior cell of each timed kernel
 CONFIG2_KERNELS = ((0, "cg_w_step", 48), (1, "cg_ur_step", 48), (4, "cheby_step", 72), (5, "ppcg_inner_sweep", 64),
-                   (6, "cheby32_step", 28), (7, "ppcg32_inner_sweep", 32))
+                   (6, "cheby32_step", 24), (7, "ppcg32_inner_sweep", 28))
 
 
 def config2_deck(n: int, solver: str) -> str:

@@ -77,23 +77,36 @@ void launch_ir_dir(tl_ctx *ctx, const float *psrc, float *pdst, int guard) {
   else launch_ir_dir_t<2>(ctx, psrc, pdst, guard, ctx->ir->walk_dir);
 }
 
-template <int AHEAD>
-void launch_ir_update_t(tl_ctx *ctx, const float *p, int guard, cudaGraphConditionalHandle cond, int set_cond,
-                        const Walk &wk) {
-  OpIrUpdate<AHEAD> op;
+template <int AHEAD, int KIND>
+void launch_sweep_t(tl_ctx *ctx, const Walk &wk, const float *src, float *a, float *b, float *out, int pp, int guard,
+                    cudaGraphConditionalHandle cond, int set_cond) {
+  OpIrSweep<AHEAD, KIND> op;
   op.F = ctx->F;
   op.g = g32_of(ctx);
-  op.q = ptrs_of(ctx);
-  op.p = p;
+  op.s = src;
+  op.iw = ctx->ir->iw;
+  op.a = a;
+  op.b = b;
+  op.out = out;
+  op.pp = pp;
   op.guard = guard;
   op.cond = cond;
   op.set_cond = set_cond;
-  k_walk32<OpIrUpdate<AHEAD>><<<wk.blocks, 32 * wk.warps, 0, ctx->stream>>>(op, wk, ctx->g.ny);
+  k_walk32<OpIrSweep<AHEAD, KIND>><<<wk.blocks, 32 * wk.warps, 0, ctx->stream>>>(op, wk, ctx->g.ny);
 }
 
+template <int KIND>
+void launch_sweep_kind(tl_ctx *ctx, const float *src, float *a, float *b, float *out, int pp, int guard,
+                       cudaGraphConditionalHandle cond, int set_cond) {
+  const int slot = KIND == SWEEP_PPCG_LAST ? SWEEP_PPCG_INNER : KIND;
+  const Walk &wk = ctx->ir->walk_sweep[slot];
+  if (ctx->ir->sweep_ahead[slot] == 1) launch_sweep_t<1, KIND>(ctx, wk, src, a, b, out, pp, guard, cond, set_cond);
+  else launch_sweep_t<2, KIND>(ctx, wk, src, a, b, out, pp, guard, cond, set_cond);
+}
+
+// The FP32 CG update step on p' (x += alpha p', r -= alpha w, r.r).
 void launch_ir_update(tl_ctx *ctx, const float *p, int guard, cudaGraphConditionalHandle cond, int set_cond) {
-  if (ctx->ir->upd_ahead == 1) launch_ir_update_t<1>(ctx, p, guard, cond, set_cond, ctx->ir->walk_upd);
-  else launch_ir_update_t<2>(ctx, p, guard, cond, set_cond, ctx->ir->walk_upd);
+  launch_sweep_kind<SWEEP_CG>(ctx, p, ctx->ir->x, ctx->ir->r, nullptr, 0, guard, cond, set_cond);
 }
 
 template <class Op>
@@ -103,12 +116,18 @@ int occupancy_of(int threads) {
   return e == cudaSuccess ? n : 1;
 }
 
-void tune_w32(tl_ctx *ctx, const Walk &wk) { launch_ir_w(ctx, ctx->ir->p, ctx->ir->pb, 0, &wk); }
-void tune_ur32(tl_ctx *ctx, const Walk &wk) { launch_ir_ur(ctx, ctx->ir->pb, 0, 0, 0, &wk); }
 void tune_dir2(tl_ctx *ctx, const Walk &wk) { launch_ir_dir_t<2>(ctx, ctx->ir->p, ctx->ir->pb, 0, wk); }
 void tune_dir1(tl_ctx *ctx, const Walk &wk) { launch_ir_dir_t<1>(ctx, ctx->ir->p, ctx->ir->pb, 0, wk); }
-void tune_upd2(tl_ctx *ctx, const Walk &wk) { launch_ir_update_t<2>(ctx, ctx->ir->pb, 0, 0, 0, wk); }
-void tune_upd1(tl_ctx *ctx, const Walk &wk) { launch_ir_update_t<1>(ctx, ctx->ir->pb, 0, 0, 0, wk); }
+
+// Tuning launches of one sweep form on the (zeroed) FP32 buffers.
+template <int AHEAD, int KIND>
+void tune_sweep(tl_ctx *ctx, const Walk &wk) {
+  tl_ir_state *ir = ctx->ir;
+  if (KIND == SWEEP_CG) launch_sweep_t<AHEAD, KIND>(ctx, wk, ir->pb, ir->x, ir->r, nullptr, 0, 0, 0, 0);
+  else if (KIND == SWEEP_PPCG_UPDATE) launch_sweep_t<AHEAD, KIND>(ctx, wk, ir->pb, ir->x, ir->r, ir->sd, 0, 0, 0, 0);
+  else if (KIND == SWEEP_CHEBY) launch_sweep_t<AHEAD, KIND>(ctx, wk, ir->sd, ir->r, ir->p, ir->sdb, 0, 0, 0, 0);
+  else launch_sweep_t<AHEAD, KIND>(ctx, wk, ir->sd, ir->r, ir->x, ir->sdb, 1, 0, 0, 0);
+}
 
 // Average time of `reps` launches of one tuned form (after two warm-up launches).
 float time_form(tl_ctx *ctx, void (*launch)(tl_ctx *, const Walk &), const Walk &wk, int reps) {
@@ -121,6 +140,21 @@ float time_form(tl_ctx *ctx, void (*launch)(tl_ctx *, const Walk &), const Walk 
     return ms;
   cudaEventElapsedTime(&ms, ctx->tev0, ctx->tev1);
   return ms / reps;
+}
+
+// Both forms of one sweep kind tuned; the faster kept (without tuning: the
+// fixed layout and the form that loads rows as reached).
+template <int KIND>
+void tune_kind(tl_ctx *ctx, bool tuning) {
+  using O2 = OpIrSweep<2, KIND>;
+  using O1 = OpIrSweep<1, KIND>;
+  const Walk w2 = tl_autotune(ctx, 128, occupancy_of<O2>(128), occupancy_of<O2>(256), tune_sweep<2, KIND>);
+  const Walk w1 = tl_autotune(ctx, 128, occupancy_of<O1>(128), occupancy_of<O1>(256), tune_sweep<1, KIND>);
+  const float t2 = tuning ? time_form(ctx, tune_sweep<2, KIND>, w2, 5) : 1.f;
+  const float t1 = tuning ? time_form(ctx, tune_sweep<1, KIND>, w1, 5) : 0.f;
+  const int ahead = (t1 >= 0.f && t2 >= 0.f && t2 < t1) ? 2 : 1;
+  ctx->ir->sweep_ahead[KIND] = ahead;
+  ctx->ir->walk_sweep[KIND] = ahead == 1 ? w1 : w2;
 }
 
 constexpr int NBUF = 10;  // FP32 arrays: kx, ky, p, pb, r, w, x, sd, sdb, iw
@@ -142,11 +176,9 @@ int ensure_ir(tl_ctx *ctx) {
   ir->sd = f[7]; ir->sdb = f[8]; ir->iw = f[9];
   // tune on the zeroed buffers, then zero them again: the trial launches
   // leave NaN behind (alpha = 0/0)
-  ir->walk_w = tl_autotune(ctx, 128, occupancy_of<OpIrW>(128), occupancy_of<OpIrW>(256), tune_w32);
-  ir->walk_ur = tl_autotune(ctx, 128, occupancy_of<OpIrUR>(128), occupancy_of<OpIrUR>(256), tune_ur32);
-  // OpIrDir, OpIrUpdate: each form tuned, then the faster one kept (without
-  // tuning, TEALEAF_GB300_TUNE=0: the fixed layout and the two-row-ahead
-  // direction step with the as-reached update step)
+  // OpIrDir and each sweep kind: both forms tuned, the faster kept (without
+  // tuning, TEALEAF_GB300_TUNE=0: the fixed layout, the direction step with
+  // rows two ahead and the sweeps with rows as reached)
   const char *tune = getenv("TEALEAF_GB300_TUNE");
   const bool tuning = !(tune && !strcmp(tune, "0"));
   const Walk d2 = tl_autotune(ctx, 128, occupancy_of<OpIrDir<2>>(128), occupancy_of<OpIrDir<2>>(256), tune_dir2);
@@ -155,12 +187,13 @@ int ensure_ir(tl_ctx *ctx) {
   const float s1 = tuning ? time_form(ctx, tune_dir1, d1, 5) : 1.f;
   ir->dir_ahead = (s1 >= 0.f && s2 >= 0.f && s1 < s2) ? 1 : 2;
   ir->walk_dir = ir->dir_ahead == 1 ? d1 : d2;
-  const Walk u2 = tl_autotune(ctx, 128, occupancy_of<OpIrUpdate<2>>(128), occupancy_of<OpIrUpdate<2>>(256), tune_upd2);
-  const Walk u1 = tl_autotune(ctx, 128, occupancy_of<OpIrUpdate<1>>(128), occupancy_of<OpIrUpdate<1>>(256), tune_upd1);
-  const float t2 = tuning ? time_form(ctx, tune_upd2, u2, 5) : 1.f;
-  const float t1 = tuning ? time_form(ctx, tune_upd1, u1, 5) : 0.f;
-  ir->upd_ahead = (t1 >= 0.f && t2 >= 0.f && t1 < t2) ? 1 : 2;
-  ir->walk_upd = ir->upd_ahead == 1 ? u1 : u2;
+  tune_kind<SWEEP_CG>(ctx, tuning);
+  tune_kind<SWEEP_PPCG_UPDATE>(ctx, tuning);
+  tune_kind<SWEEP_CHEBY>(ctx, tuning);
+  tune_kind<SWEEP_PPCG_INNER>(ctx, tuning);
+  // the 48-byte pair (kept for comparison in tl_bench_kernel) on the same layouts
+  ir->walk_w = ir->walk_dir;
+  ir->walk_ur = ir->walk_sweep[SWEEP_CG];
   cudaGetLastError();
   CK(cudaMemsetAsync(ir->buf, 0, sizeof(float) * ir->stride * NBUF, ctx->stream));
   return TL_OK;
@@ -406,7 +439,7 @@ tl::Walk *tl_ir_walk(tl_ctx *ctx, int kernel) {
     case 2: return &ctx->ir->walk_w;
     case 3: return &ctx->ir->walk_ur;
     case 8: return &ctx->ir->walk_dir;
-    case 9: return &ctx->ir->walk_upd;
+    case 9: return &ctx->ir->walk_sweep[SWEEP_CG];
     default: return nullptr;
   }
 }
@@ -418,143 +451,13 @@ tl::Walk *tl_ir_walk(tl_ctx *ctx, int kernel) {
 namespace tl {
 namespace {
 
-// One FP32 Chebyshev step on the correction e of the current refinement
-// (A e = r0): w = A e (difference form, reflective boundary in the index
-// math), r = r0 - w, p = alpha_k p + beta_k r, e' = e + p, and r.r (each
-// lane's four products summed in FP32, accumulated in FP64).  The epilogue
-// counts the step and asks for a refinement once r.r has dropped by delta^2
-// or claims convergence.
-struct OpCheby32 {
-  static constexpr bool REDUCES = true;
-  Fields F;
-  G32 g;
-  IrPtrs q;  // kx, ky, r (= r0)
-  const float *__restrict__ esrc;
-  float *__restrict__ edst;
-  float *__restrict__ p;
-  int guard;
-  __device__ bool skip() const { return guard && F.sc->done; }
-  __device__ void on_skip() const {}
-
-  // The per-row operands other than e, loaded one row ahead of their use.
-  struct Row {
-    float4 kx, r0, p;
-    float ew, ee, kxe;  // west edge (lane 0), east edge and its kx (lane 31 or the last column)
-  };
-  __device__ __forceinline__ void load_row(Row &o, int i0, int j, bool valid, bool full, bool inner, int lane) const {
-    if (!valid) return;
-    const size_t c = g.at(i0, j);
-    o.kx = ld4(q.kx + c);
-    o.r0 = ld4(q.r + c);
-    o.p = ld4(p + c);
-    if (lane == 0 && i0 > 0) o.ew = __ldg(esrc + c - 1);
-    if (full && (lane == 31 || !inner)) {
-      o.kxe = __ldg(q.kx + c + 4);
-      if (inner) o.ee = __ldg(esrc + c + 4);
-    }
-  }
-
-  __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
-    const int nx = g.nx, ny = g.ny;
-    const int lane = threadIdx.x & 31;
-    const bool valid = i0 < nx;
-    const int ncell = valid ? min(4, nx - i0) : 0;
-    const bool full = ncell == 4;
-    const bool inner = i0 + 4 < nx;
-    const int k = F.sc->cheby_iters + 1;
-    const int idx = min(k + 1, F.sc->maxiters + 1);
-    const float ca = (float)F.chebyalpha[idx], cb = (float)F.chebybeta[idx];
-    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-    auto ld = [&](const float *a, int j) { return valid ? ld4(a + g.at(i0, j)) : z; };
-    float4 ec = ld(esrc, j0);
-    float4 es = j0 > 0 ? ld(esrc, j0 - 1) : ec;
-    float4 en = j0 + 1 < ny ? ld(esrc, j0 + 1) : ec;
-    float4 kys = ld(q.ky, j0), kyn = ld(q.ky, j0 + 1);
-    Row cur = {}, nxt = {};
-    load_row(cur, i0, j0, valid, full, inner, lane);
-    for (int j = j0; j < j1; ++j) {
-      // next row's operands, and e and ky two rows ahead
-      float4 enn = z, kynn = z;
-      if (j + 1 < j1) {
-        load_row(nxt, i0, j + 1, valid, full, inner, lane);
-        if (j + 2 < ny) enn = ld(esrc, j + 2);
-        kynn = ld(q.ky, j + 2);
-      }
-      float ew = __shfl_up_sync(FULL, ec.w, 1);
-      float ee = __shfl_down_sync(FULL, ec.x, 1);
-      float kxe = __shfl_down_sync(FULL, cur.kx.x, 1);
-      float a = 0.f;
-      if (valid) {
-        if (i0 == 0) ew = ec.x;
-        else if (lane == 0) ew = cur.ew;
-        if (full && (lane == 31 || !inner)) {
-          kxe = cur.kxe;
-          ee = inner ? cur.ee : ec.w;
-        }
-        float pn[4], en4[4];
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-          pn[m] = 0.f;
-          en4[m] = 0.f;
-          if (m < ncell) {
-            const float c = comp(ec, m);
-            const float e = (m + 1 < ncell) ? comp(ec, m + 1) : (m == 3 ? ee : c);
-            const float wl = (m == 0) ? ew : comp(ec, m - 1);
-            const float k1 = (m == 3) ? kxe : comp(cur.kx, m + 1);
-            float w = c;
-            w = fmaf(k1, c - e, w);
-            w = fmaf(comp(cur.kx, m), c - wl, w);
-            w = fmaf(comp(kyn, m), c - comp(en, m), w);
-            w = fmaf(comp(kys, m), c - comp(es, m), w);
-            const float r = comp(cur.r0, m) - w;
-            pn[m] = fmaf(ca, comp(cur.p, m), cb * r);
-            en4[m] = c + pn[m];
-            a = fmaf(r, r, a);
-          }
-        }
-        const size_t c0 = g.at(i0, j);
-        if (full) {
-          st4(p + c0, make_float4(pn[0], pn[1], pn[2], pn[3]));
-          st4(edst + c0, make_float4(en4[0], en4[1], en4[2], en4[3]));
-        } else {
-          for (int m = 0; m < ncell; ++m) {
-            p[c0 + m] = pn[m];
-            edst[c0 + m] = en4[m];
-          }
-        }
-      }
-      acc[0] += (double)a;
-      es = ec;
-      ec = en;
-      en = (j + 2 < ny) ? enn : ec;
-      kys = kyn;
-      kyn = kynn;
-      cur = nxt;
-    }
-  }
-  __device__ void fin(const double *tot) const {
-    DevScalars *sc = F.sc;
-    const double rr = tot[0];
-    sc->cheby_iters += 1;
-    sc->iter += 1;
-    sc->error = rr;
-    const bool claim = sqrt(rr / sc->bb) < sc->eps;
-    const bool refine = claim || rr < sc->delta2 * sc->rr_ref;
-    sc->converged = 0;
-    sc->switched = refine;
-    sc->done = refine || sc->iter >= sc->maxiters;
-  }
-};
-
-// FP32 copies for the Chebyshev phase: kx, ky (whole arrays), p (interior);
-// both correction buffers zeroed.
-__global__ void k_cheby32_convert(Fields F, Geom g, G32 g32, float *kx, float *ky, float *p, float *e0, float *e1) {
+// The start of the FP32 Chebyshev phase: p32 = (float) p (the first
+// Chebyshev step's p) and both correction buffers zeroed.
+__global__ void k_cheby32_convert(Fields F, Geom g, G32 g32, float *p, float *e0, float *e1) {
   const long long n = (long long)g.X * g.Y;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
     const int I = (int)(k % g.X), J = (int)(k / g.X);
     const size_t c = (size_t)I + (size_t)J * g.pitch, c32 = (size_t)I + (size_t)J * g32.pitch;
-    kx[c32] = (float)F.kx[c];
-    ky[c32] = (float)F.ky[c];
     const bool interior = I >= g.hd && I < g.X - g.hd && J >= g.hd && J < g.Y - g.hd;
     p[c32] = interior ? (float)F.p[c] : 0.f;
     e0[c32] = 0.f;
@@ -562,17 +465,10 @@ __global__ void k_cheby32_convert(Fields F, Geom g, G32 g32, float *kx, float *k
   }
 }
 
+// One FP32 Chebyshev step on the correction (the sweep of kind SWEEP_CHEBY):
+// r = r0 - A e, p = alpha_k p + beta_k r, e' = e + p, r.r.
 void launch_cheby32(tl_ctx *ctx, const float *esrc, float *edst, int guard) {
-  OpCheby32 op;
-  op.F = ctx->F;
-  op.g = g32_of(ctx);
-  op.q = ptrs_of(ctx);
-  op.esrc = esrc;
-  op.edst = edst;
-  op.p = ctx->ir->p;
-  op.guard = guard;
-  const Walk &wk = ctx->ir->walk_w;
-  k_walk32<OpCheby32><<<wk.blocks, 32 * wk.warps, 0, ctx->stream>>>(op, wk, ctx->g.ny);
+  launch_sweep_kind<SWEEP_CHEBY>(ctx, esrc, ctx->ir->r, ctx->ir->p, edst, 0, guard, 0, 0);
 }
 
 }  // namespace
@@ -596,8 +492,8 @@ int tl_cheby32_run(tl_ctx *ctx, const tl_params *prm, int *refinements, double *
     launch_copy_interior(ctx->stream, ctx->F.u, ctx->F.ub, ctx->g);
     CKL();
   }
-  k_cheby32_convert<<<grid_for((long long)ctx->g.X * ctx->g.Y), 256, 0, ctx->stream>>>(ctx->F, ctx->g, g32, ir->kx,
-                                                                                       ir->ky, ir->p, ir->x, ir->pb);
+  k_cheby32_convert<<<grid_for((long long)ctx->g.X * ctx->g.Y), 256, 0, ctx->stream>>>(ctx->F, ctx->g, g32, ir->p,
+                                                                                       ir->x, ir->pb);
   CKL();
   double rr;
   if ((rc = refine(ctx, &rr))) return rc;  // x = 0: the halo of u and the true residual
@@ -645,214 +541,24 @@ int tl_cheby32_run(tl_ctx *ctx, const tl_params *prm, int *refinements, double *
 namespace tl {
 namespace {
 
-// PPCG's update after the W step (PPCG.jl:64-72 with the tealeaf-mode start
-// of the inner sweeps): x += alpha p', r -= alpha w, sd = r / theta.
-struct OpPpcg32UR {
-  static constexpr bool REDUCES = false;
-  Fields F;
-  G32 g;
-  IrPtrs q;
-  const float *__restrict__ p;
-  float *__restrict__ sd;
-  int guard;
-  __device__ bool skip() const { return guard && F.sc->done; }
-  __device__ void on_skip() const {}
-  __device__ void tile(int i0, int j0, int j1, double (&)[1]) const {
-    if (i0 >= g.nx) return;
-    const int ncell = min(4, g.nx - i0);
-    const float alpha = (float)F.sc->alpha, theta = (float)F.sc->theta;
-    for (int j = j0; j < j1; ++j) {
-      const size_t c = g.at(i0, j);
-      if (ncell == 4) {
-        const float4 pv = ld4(p + c), wv = ld4(q.w + c);
-        float4 xv = ld4(q.x + c), rv = ld4(q.r + c);
-        xv.x = fmaf(alpha, pv.x, xv.x); xv.y = fmaf(alpha, pv.y, xv.y);
-        xv.z = fmaf(alpha, pv.z, xv.z); xv.w = fmaf(alpha, pv.w, xv.w);
-        rv.x = fmaf(-alpha, wv.x, rv.x); rv.y = fmaf(-alpha, wv.y, rv.y);
-        rv.z = fmaf(-alpha, wv.z, rv.z); rv.w = fmaf(-alpha, wv.w, rv.w);
-        st4(q.x + c, xv);
-        st4(q.r + c, rv);
-        st4(sd + c, make_float4(rv.x / theta, rv.y / theta, rv.z / theta, rv.w / theta));
-      } else {
-        for (int k = 0; k < ncell; ++k) {
-          q.x[c + k] = fmaf(alpha, p[c + k], q.x[c + k]);
-          const float rv = fmaf(-alpha, q.w[c + k], q.r[c + k]);
-          q.r[c + k] = rv;
-          sd[c + k] = rv / theta;
-        }
-      }
-    }
-  }
-  __device__ void fin(const double *) const {}
-};
+// PPCG's update after the direction step (PPCG.jl:64-72 with the
+// tealeaf-mode start of the inner sweeps): x += alpha p', r -= alpha A p',
+// sd = r / theta.
+void launch_ppcg32_ur(tl_ctx *ctx, const float *p, int guard) {
+  tl_ir_state *ir = ctx->ir;
+  launch_sweep_kind<SWEEP_PPCG_UPDATE>(ctx, p, ir->x, ir->r, ir->sd, 0, guard, 0, 0);
+}
 
 // One PPCG inner sweep in FP32 (PPCG.jl:74-88, the halo of sd reflected in
 // the index math): r -= A sd, x += sd, sd' = alpha_pp sd + beta_pp r.  The
-// last sweep of an outer step also sums r.r and runs the outer step's
-// epilogue (beta, the iteration count, the refinement test).
-template <bool LAST>
-struct OpPpcg32Inner {
-  static constexpr bool REDUCES = LAST;
-  Fields F;
-  G32 g;
-  IrPtrs q;  // kx, ky, r, x
-  const float *__restrict__ sdsrc;
-  float *__restrict__ sddst;
-  int pp;  // 1-based inner sweep
-  int guard;
-  cudaGraphConditionalHandle cond;
-  int set_cond;
-  __device__ bool skip() const { return guard && F.sc->done; }
-  __device__ void on_skip() const {
-    if (set_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0u);
-  }
-
-  // The per-row operands other than sd, loaded one row ahead of their use.
-  struct Row {
-    float4 kx, r, x;
-    float sw, se, kxe;  // west edge (lane 0), east edge and its kx (lane 31 or the last column)
-  };
-  __device__ __forceinline__ void load_row(Row &o, int i0, int j, bool valid, bool full, bool inner, int lane) const {
-    if (!valid) return;
-    const size_t c = g.at(i0, j);
-    o.kx = ld4(q.kx + c);
-    o.r = ld4(q.r + c);
-    o.x = ld4(q.x + c);
-    if (lane == 0 && i0 > 0) o.sw = __ldg(sdsrc + c - 1);
-    if (full && (lane == 31 || !inner)) {
-      o.kxe = __ldg(q.kx + c + 4);
-      if (inner) o.se = __ldg(sdsrc + c + 4);
-    }
-  }
-
-  __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
-    const int nx = g.nx, ny = g.ny;
-    const int lane = threadIdx.x & 31;
-    const bool valid = i0 < nx;
-    const int ncell = valid ? min(4, nx - i0) : 0;
-    const bool full = ncell == 4;
-    const bool inner = i0 + 4 < nx;
-    const float ca = (float)F.chebyalpha[pp], cb = (float)F.chebybeta[pp];
-    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-    auto ld = [&](const float *a, int j) { return valid ? ld4(a + g.at(i0, j)) : z; };
-    float4 sc = ld(sdsrc, j0);
-    float4 ss = j0 > 0 ? ld(sdsrc, j0 - 1) : sc;
-    float4 sn = j0 + 1 < ny ? ld(sdsrc, j0 + 1) : sc;
-    float4 kys = ld(q.ky, j0), kyn = ld(q.ky, j0 + 1);
-    Row cur = {}, nxt = {};
-    load_row(cur, i0, j0, valid, full, inner, lane);
-    for (int j = j0; j < j1; ++j) {
-      // next row's operands, and sd and ky two rows ahead
-      float4 snn = z, kynn = z;
-      if (j + 1 < j1) {
-        load_row(nxt, i0, j + 1, valid, full, inner, lane);
-        if (j + 2 < ny) snn = ld(sdsrc, j + 2);
-        kynn = ld(q.ky, j + 2);
-      }
-      float sw = __shfl_up_sync(FULL, sc.w, 1);
-      float se = __shfl_down_sync(FULL, sc.x, 1);
-      float kxe = __shfl_down_sync(FULL, cur.kx.x, 1);
-      float a = 0.f;
-      if (valid) {
-        if (i0 == 0) sw = sc.x;
-        else if (lane == 0) sw = cur.sw;
-        if (full && (lane == 31 || !inner)) {
-          kxe = cur.kxe;
-          se = inner ? cur.se : sc.w;
-        }
-        float rn[4], xn[4], sdn[4];
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-          rn[m] = 0.f;
-          xn[m] = 0.f;
-          sdn[m] = 0.f;
-          if (m < ncell) {
-            const float c = comp(sc, m);
-            const float e = (m + 1 < ncell) ? comp(sc, m + 1) : (m == 3 ? se : c);
-            const float wl = (m == 0) ? sw : comp(sc, m - 1);
-            const float k1 = (m == 3) ? kxe : comp(cur.kx, m + 1);
-            float w = c;
-            w = fmaf(k1, c - e, w);
-            w = fmaf(comp(cur.kx, m), c - wl, w);
-            w = fmaf(comp(kyn, m), c - comp(sn, m), w);
-            w = fmaf(comp(kys, m), c - comp(ss, m), w);
-            const float r = comp(cur.r, m) - w;
-            rn[m] = r;
-            xn[m] = comp(cur.x, m) + c;
-            sdn[m] = fmaf(ca, c, cb * r);
-            if (LAST) a = fmaf(r, r, a);
-          }
-        }
-        const size_t c0 = g.at(i0, j);
-        if (full) {
-          st4(q.r + c0, make_float4(rn[0], rn[1], rn[2], rn[3]));
-          st4(q.x + c0, make_float4(xn[0], xn[1], xn[2], xn[3]));
-          st4(sddst + c0, make_float4(sdn[0], sdn[1], sdn[2], sdn[3]));
-        } else {
-          for (int m = 0; m < ncell; ++m) {
-            q.r[c0 + m] = rn[m];
-            q.x[c0 + m] = xn[m];
-            sddst[c0 + m] = sdn[m];
-          }
-        }
-      }
-      if (LAST) acc[0] += (double)a;
-      ss = sc;
-      sc = sn;
-      sn = (j + 2 < ny) ? snn : sc;
-      kys = kyn;
-      kyn = kynn;
-      cur = nxt;
-    }
-  }
-  __device__ void fin(const double *tot) const {
-    if (!LAST) return;
-    DevScalars *sc = F.sc;
-    const double rrn = tot[0];
-    sc->beta = rrn / sc->rro;  // PPCG.jl:89-92
-    sc->rro = rrn;
-    sc->error = rrn;
-    sc->iter += 1;
-    sc->cheby_iters += 1;
-    sc->first = 0;
-    const bool claim = sqrt(rrn / sc->bb) < sc->eps;
-    const bool refine = claim || rrn < sc->delta2 * sc->rr_ref;
-    sc->converged = 0;
-    sc->switched = refine;
-    const int done = refine || sc->iter >= sc->maxiters;
-    sc->done = done;
-    if (set_cond) cudaGraphSetConditional(cond, done ? 0u : 1u);
-  }
-};
-
-void launch_ppcg32_ur(tl_ctx *ctx, const float *p, int guard) {
-  OpPpcg32UR op;
-  op.F = ctx->F;
-  op.g = g32_of(ctx);
-  op.q = ptrs_of(ctx);
-  op.p = p;
-  op.sd = ctx->ir->sd;
-  op.guard = guard;
-  const Walk &wk = ctx->ir->walk_ur;
-  k_walk32<OpPpcg32UR><<<wk.blocks, 32 * wk.warps, 0, ctx->stream>>>(op, wk, ctx->g.ny);
-}
-
+// last sweep of an outer step also sums r.r and closes the step (beta, the
+// iteration count, the refinement test).
 void launch_ppcg32_inner(tl_ctx *ctx, int pp, int last, int guard, cudaGraphConditionalHandle cond, int set_cond) {
   tl_ir_state *ir = ctx->ir;
   const float *src = (pp & 1) ? ir->sd : ir->sdb;
   float *dst = (pp & 1) ? ir->sdb : ir->sd;
-  const Walk &wk = ir->walk_w;
-  if (last) {
-    OpPpcg32Inner<true> op;
-    op.F = ctx->F; op.g = g32_of(ctx); op.q = ptrs_of(ctx); op.sdsrc = src; op.sddst = dst; op.pp = pp;
-    op.guard = guard; op.cond = cond; op.set_cond = set_cond;
-    k_walk32<OpPpcg32Inner<true>><<<wk.blocks, 32 * wk.warps, 0, ctx->stream>>>(op, wk, ctx->g.ny);
-  } else {
-    OpPpcg32Inner<false> op;
-    op.F = ctx->F; op.g = g32_of(ctx); op.q = ptrs_of(ctx); op.sdsrc = src; op.sddst = dst; op.pp = pp;
-    op.guard = guard; op.cond = 0; op.set_cond = 0;
-    k_walk32<OpPpcg32Inner<false>><<<wk.blocks, 32 * wk.warps, 0, ctx->stream>>>(op, wk, ctx->g.ny);
-  }
+  if (last) launch_sweep_kind<SWEEP_PPCG_LAST>(ctx, src, ir->r, ir->x, dst, pp, guard, cond, set_cond);
+  else launch_sweep_kind<SWEEP_PPCG_INNER>(ctx, src, ir->r, ir->x, dst, pp, guard, 0, 0);
 }
 
 // One PPCG outer step in FP32: W (p' = beta p + r, w = A p', alpha), the
@@ -861,7 +567,7 @@ void launch_ppcg32_inner(tl_ctx *ctx, int pp, int last, int guard, cudaGraphCond
 void ppcg32_outer(tl_ctx *ctx, int which, int n, int guard, cudaGraphConditionalHandle cond, int set_cond) {
   tl_ir_state *ir = ctx->ir;
   float *a = which ? ir->pb : ir->p, *b = which ? ir->p : ir->pb;
-  launch_ir_w(ctx, a, b, guard);
+  launch_ir_dir(ctx, a, b, guard);
   launch_ppcg32_ur(ctx, b, 1);
   for (int pp = 1; pp <= n; ++pp) launch_ppcg32_inner(ctx, pp, pp == n, 1, cond, pp == n && set_cond);
 }

@@ -19,8 +19,10 @@ struct tl_ir_state {
   float *sd = nullptr, *sdb = nullptr;  // PPCG inner sweeps: the update and its second buffer
   float *iw = nullptr;                  // 1 / w (w = rho or 1/rho, CG.jl:57-60), halo included
   tl::Walk walk_w{}, walk_ur{};    // autotuned layouts of OpIrW, OpIrUR (and the Chebyshev/PPCG sweeps)
-  tl::Walk walk_dir{}, walk_upd{};  // autotuned layouts of OpIrDir, OpIrUpdate (the CG iteration)
-  int upd_ahead = 2, dir_ahead = 2;  // the faster OpIrUpdate / OpIrDir form after tuning (its AHEAD)
+  tl::Walk walk_dir{};              // autotuned layout of OpIrDir
+  tl::Walk walk_sweep[4]{};         // autotuned layouts of OpIrSweep, by kind (the last inner sweep shares slot 3)
+  int dir_ahead = 2;                // the faster OpIrDir form after tuning (its AHEAD)
+  int sweep_ahead[4] = {1, 1, 1, 1};
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // p in the first / second buffer
   cudaGraphExec_t ppcg_graph[2] = {nullptr, nullptr};
   int ppcg_inner = -1;  // inner sweeps recorded in ppcg_graph
@@ -448,18 +450,38 @@ struct OpIrDir {
   }
 };
 
-// w = A p' (recomputed from the stored p'), x += alpha p', r -= alpha w, r.r;
-// the epilogue is OpIrUR's (the refinement test, the Chebyshev switch test
-// as presteps).  AHEAD: the stencil rows are loaded two rows ahead of their
-// use (2) or as the row is reached (1, fewer registers and more resident
-// warps); x and r are loaded one row ahead in both.
-template <int AHEAD>
-struct OpIrUpdate {
-  static constexpr bool REDUCES = true;
+// The sweep kernels: a five-point stencil w = A s on one FP32 field s (from
+// the inverse weights) and an update of two own-cell operands (a, b), with
+// up to three stores.  KIND:
+//   SWEEP_CG          s = p', a = x, b = r:  x += alpha p', r -= alpha w, r.r
+//                     (the FP32 CG update step; the epilogue decides between
+//                     another step and a refinement)
+//   SWEEP_PPCG_UPDATE s = p', a = x, b = r:  the same, then sd = r / theta
+//                     (PPCG.jl:64-72), no reduction
+//   SWEEP_CHEBY       s = e, a = r0, b = p:  r = r0 - w, p = alpha_k p + beta_k r,
+//                     e' = e + p into `out`, r.r (one Chebyshev step on the
+//                     correction of the current refinement)
+//   SWEEP_PPCG_INNER  s = sd, a = r, b = x: r -= w, x += sd,
+//                     sd' = alpha_pp sd + beta_pp r into `out` (one inner
+//                     sweep, PPCG.jl:74-88); the last sweep (LAST) also sums
+//                     r.r and closes the outer step
+// AHEAD: the stencil rows are loaded two rows ahead of their use (2) or as
+// the row is reached (1: fewer registers, more resident warps); a and b are
+// loaded one row ahead in both.
+enum { SWEEP_CG = 0, SWEEP_PPCG_UPDATE = 1, SWEEP_CHEBY = 2, SWEEP_PPCG_INNER = 3, SWEEP_PPCG_LAST = 4 };
+
+template <int AHEAD, int KIND>
+struct OpIrSweep {
+  static constexpr bool REDUCES = KIND == SWEEP_CG || KIND == SWEEP_CHEBY || KIND == SWEEP_PPCG_LAST;
+  static constexpr bool INNER = KIND == SWEEP_PPCG_INNER || KIND == SWEEP_PPCG_LAST;
   Fields F;
   G32 g;
-  IrPtrs q;
-  const float *__restrict__ p;
+  const float *__restrict__ s;   // the stencil field
+  const float *__restrict__ iw;  // inverse weights
+  float *__restrict__ a;         // own-cell operands (updated in place, except r0)
+  float *__restrict__ b;
+  float *__restrict__ out;       // sd (PPCG update), e' (Chebyshev), sd' (inner sweep)
+  int pp;                        // inner sweep (1-based)
   int guard;
   cudaGraphConditionalHandle cond;
   int set_cond;
@@ -469,21 +491,21 @@ struct OpIrUpdate {
   }
 
   struct Nb {  // the stencil operands of one row
-    float4 p, iw;
-    float pw, pe, iww, iwe;
+    float4 s, iw;
+    float sw, se, iww, iwe;
   };
   __device__ __forceinline__ void load_nb(Nb &o, int i0, int j, bool valid, int lane, bool inner) const {
     if (!valid) return;
     const size_t c = g.at(i0, j);
-    o.p = ld4(p + c);
-    o.iw = ld4(q.iw + c);
+    o.s = ld4(s + c);
+    o.iw = ld4(iw + c);
     if (lane == 0 && i0 > 0) {
-      o.pw = __ldg(p + c - 1);
-      o.iww = __ldg(q.iw + c - 1);
+      o.sw = __ldg(s + c - 1);
+      o.iww = __ldg(iw + c - 1);
     }
     if (lane == 31 && inner) {
-      o.pe = __ldg(p + c + 4);
-      o.iwe = __ldg(q.iw + c + 4);
+      o.se = __ldg(s + c + 4);
+      o.iwe = __ldg(iw + c + 4);
     }
   }
 
@@ -494,17 +516,29 @@ struct OpIrUpdate {
     const int ncell = valid ? min(4, nx - i0) : 0;
     const bool full = ncell == 4;
     const bool inner = i0 + 4 < nx;
-    const float alpha = (float)F.sc->alpha;
-    const float rxh = (float)F.sc->rxh, ryh = (float)F.sc->ryh;
+    const DevScalars *sc = F.sc;
+    const float rxh = (float)sc->rxh, ryh = (float)sc->ryh;
+    float c0 = 0.f, c1 = 0.f;  // alpha (CG, PPCG update) / 1/theta; or the Chebyshev pair
+    if (KIND == SWEEP_CG || KIND == SWEEP_PPCG_UPDATE) {
+      c0 = (float)sc->alpha;
+      c1 = (float)sc->theta;
+    } else if (KIND == SWEEP_CHEBY) {
+      const int idx = min(sc->cheby_iters + 2, sc->maxiters + 1);
+      c0 = (float)F.chebyalpha[idx];
+      c1 = (float)F.chebybeta[idx];
+    } else {
+      c0 = (float)F.chebyalpha[pp];
+      c1 = (float)F.chebybeta[pp];
+    }
     const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-    auto ld = [&](const float *a, int j) { return valid ? ld4(a + g.at(i0, j)) : z; };
+    auto ld = [&](const float *f, int j) { return valid ? ld4(f + g.at(i0, j)) : z; };
     Nb cur = {}, nxt = {};
     load_nb(cur, i0, j0, valid, lane, inner);
-    float4 xc = ld(q.x, j0), rc = ld(q.r, j0);
-    float4 ps = (j0 > 0 && valid) ? ld(p, j0 - 1) : cur.p;
-    float4 is = (j0 > 0 && valid) ? ld(q.iw, j0 - 1) : cur.iw;
+    float4 ac = ld(a, j0), bc = ld(b, j0);
+    float4 ss = (j0 > 0 && valid) ? ld(s, j0 - 1) : cur.s;
+    float4 is = (j0 > 0 && valid) ? ld(iw, j0 - 1) : cur.iw;
     if (AHEAD == 2 && j0 + 1 < ny) load_nb(nxt, i0, j0 + 1, valid, lane, inner);
-    double a = acc[0];
+    double racc = acc[0];
     for (int j = j0; j < j1; ++j) {
       Nb nn = {};
       if (AHEAD == 2) {
@@ -512,53 +546,107 @@ struct OpIrUpdate {
       } else if (j + 1 < ny) {
         load_nb(nxt, i0, j + 1, valid, lane, inner);
       }
-      float4 xn = z, rn = z;
+      float4 an = z, bn = z;
       if (j + 1 < j1) {
-        xn = ld(q.x, j + 1);
-        rn = ld(q.r, j + 1);
+        an = ld(a, j + 1);
+        bn = ld(b, j + 1);
       }
       const bool has_n = j + 1 < ny;
-      Hood4 hp, hi;
-      hp.c = cur.p; hp.s = ps; hp.n = has_n ? nxt.p : cur.p;
+      Hood4 hs, hi;
+      hs.c = cur.s; hs.s = ss; hs.n = has_n ? nxt.s : cur.s;
       hi.c = cur.iw; hi.s = is; hi.n = has_n ? nxt.iw : cur.iw;
-      edges4(cur.p, cur.pw, cur.pe, i0, lane, full, inner, hp.w, hp.e);
+      edges4(cur.s, cur.sw, cur.se, i0, lane, full, inner, hs.w, hs.e);
       edges4(cur.iw, cur.iww, cur.iwe, i0, lane, full, inner, hi.w, hi.e);
       if (valid) {
         float wv[4];
-        stencil4(hp, hi, rxh, ryh, ncell, wv);
-        float xv[4], rv[4];
+        stencil4(hs, hi, rxh, ryh, ncell, wv);
+        float va[4], vb[4], vo[4];
         float part = 0.f;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          xv[k] = fmaf(alpha, comp(cur.p, k), comp(xc, k));
-          rv[k] = fmaf(-alpha, wv[k], comp(rc, k));
-          if (k < ncell) part = fmaf(rv[k], rv[k], part);
+          const float sv = comp(cur.s, k), av = comp(ac, k), bv = comp(bc, k);
+          float rr;
+          if (KIND == SWEEP_CG || KIND == SWEEP_PPCG_UPDATE) {
+            va[k] = fmaf(c0, sv, av);        // x + alpha p'
+            vb[k] = fmaf(-c0, wv[k], bv);    // r - alpha w
+            vo[k] = vb[k] / c1;              // sd = r / theta
+            rr = vb[k];
+          } else if (KIND == SWEEP_CHEBY) {
+            const float r = av - wv[k];      // r0 - w
+            vb[k] = fmaf(c0, bv, c1 * r);    // alpha_k p + beta_k r
+            vo[k] = sv + vb[k];              // e + p
+            va[k] = av;
+            rr = r;
+          } else {
+            va[k] = av - wv[k];              // r - w
+            vb[k] = bv + sv;                 // x + sd
+            vo[k] = fmaf(c0, sv, c1 * va[k]);
+            rr = va[k];
+          }
+          if (REDUCES && k < ncell) part = fmaf(rr, rr, part);
         }
-        a += (double)part;
-        const size_t c0 = g.at(i0, j);
+        if (REDUCES) racc += (double)part;
+        const size_t o = g.at(i0, j);
+        const bool st_a = KIND != SWEEP_CHEBY, st_o = KIND != SWEEP_CG;
         if (full) {
-          st4(q.x + c0, make_float4(xv[0], xv[1], xv[2], xv[3]));
-          st4(q.r + c0, make_float4(rv[0], rv[1], rv[2], rv[3]));
+          if (st_a) st4(a + o, make_float4(va[0], va[1], va[2], va[3]));
+          st4(b + o, make_float4(vb[0], vb[1], vb[2], vb[3]));
+          if (st_o) st4(out + o, make_float4(vo[0], vo[1], vo[2], vo[3]));
         } else {
 #pragma unroll
           for (int k = 0; k < 4; ++k)
             if (k < ncell) {
-              q.x[c0 + k] = xv[k];
-              q.r[c0 + k] = rv[k];
+              if (st_a) a[o + k] = va[k];
+              b[o + k] = vb[k];
+              if (st_o) out[o + k] = vo[k];
             }
         }
       }
-      ps = cur.p;
+      ss = cur.s;
       is = cur.iw;
       cur = nxt;
       if (AHEAD == 2) nxt = nn;
-      xc = xn;
-      rc = rn;
+      ac = an;
+      bc = bn;
     }
-    acc[0] = a;
+    acc[0] = racc;
   }
-  __device__ void fin(const double *tot) const { ir_cg_epilogue(F, tot[0], cond, set_cond); }
+  __device__ void fin(const double *tot) const {
+    if (KIND == SWEEP_CG) {
+      ir_cg_epilogue(F, tot[0], cond, set_cond);
+    } else if (KIND == SWEEP_CHEBY) {
+      DevScalars *sc = F.sc;
+      const double rr = tot[0];
+      sc->cheby_iters += 1;
+      sc->iter += 1;
+      sc->error = rr;
+      const bool claim = sqrt(rr / sc->bb) < sc->eps;
+      const bool refine = claim || rr < sc->delta2 * sc->rr_ref;
+      sc->converged = 0;
+      sc->switched = refine;
+      sc->done = refine || sc->iter >= sc->maxiters;
+    } else if (KIND == SWEEP_PPCG_LAST) {
+      DevScalars *sc = F.sc;
+      const double rrn = tot[0];
+      sc->beta = rrn / sc->rro;  // PPCG.jl:89-92
+      sc->rro = rrn;
+      sc->error = rrn;
+      sc->iter += 1;
+      sc->cheby_iters += 1;
+      sc->first = 0;
+      const bool claim = sqrt(rrn / sc->bb) < sc->eps;
+      const bool refine = claim || rrn < sc->delta2 * sc->rr_ref;
+      sc->converged = 0;
+      sc->switched = refine;
+      const int done = refine || sc->iter >= sc->maxiters;
+      sc->done = done;
+      if (set_cond) cudaGraphSetConditional(cond, done ? 0u : 1u);
+    }
+  }
 };
+
+template <int AHEAD>
+using OpIrUpdate = OpIrSweep<AHEAD, SWEEP_CG>;
 
 // Refinement: u += x, x = 0 on the interior.
 __global__ void k_ir_fold(Fields F, Geom g, G32 g32, float *x) {
