@@ -194,13 +194,12 @@ int tl_timer_start(tl_ctx *ctx);
 int tl_timer_stop(tl_ctx *ctx, double *ms);
 
 /* Times `reps` back-to-back launches of one fused iteration kernel (0: the CG
- * p-update + stencil + p.w step, 1: the u/r update + r.r step, 2: the FP32
- * stencil step, 3: the FP32 update step, 4: the Chebyshev step, 5: a PPCG
- * inner sweep, 6: the FP32 Chebyshev step, 7: an FP32 PPCG inner sweep,
- * 8: the FP32 CG direction step p' = beta p + r with p'.A p', 9: the FP32
- * CG update step with A p' recomputed; 8 and 9 are the FP32 CG iteration,
- * 2 and 3 its 48-byte form kept for PPCG and the batch) on the current
- * fields; for roofline measurements.  The launches overwrite
+ * p-update + stencil + p.w step, 1: the u/r update + r.r step, 4: the
+ * Chebyshev step, 5: a PPCG inner sweep, 6: the FP32 Chebyshev step, 7: an
+ * FP32 PPCG inner sweep, 8: the FP32 CG direction step p' = beta p + r with
+ * p'.A p', 9: the FP32 CG update step with A p' recomputed; 8 and 9 are the
+ * FP32 CG iteration; 2 and 3, an earlier FP32 pair, are retired and return
+ * TL_ERR_ARG) on the current fields; for roofline measurements.  The launches overwrite
  * solver work fields (p, w, r, u, sd, their second buffers and the FP32
  * copies): call it after the solves whose fields matter. */
 int tl_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch);

@@ -385,7 +385,11 @@ extern "C" int tl_timer_stop(tl_ctx *ctx, double *ms) {
 extern "C" int tl_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch) {
   if (!ctx || !ms_per_launch || reps < 1 || ctx->cfg.mode != TL_MODE_TEALEAF) return TL_ERR_ARG;
   const Fields &F = ctx->F;
-  if (kernel == 2 || kernel == 3 || (kernel >= 6 && kernel <= 9)) return tl_ir_bench_kernel(ctx, kernel, reps, ms_per_launch);
+  if (kernel >= 6 && kernel <= 9) return tl_ir_bench_kernel(ctx, kernel, reps, ms_per_launch);
+  if (kernel == 2 || kernel == 3) {
+    tl_set_error(ctx, "kernel %d: the 48-byte FP32 pair is retired (8 and 9 are the FP32 CG iteration)", kernel);
+    return TL_ERR_ARG;
+  }
   if (kernel < 0 || kernel > 5) return TL_ERR_ARG;
   launch_init_diag(ctx->stream, F, ctx->g);
   CKL();
@@ -414,8 +418,6 @@ static Walk *layout_of(tl_ctx *ctx, int kernel) {
   switch (kernel) {
     case 0: return &ctx->walk_w64;
     case 1: return &ctx->walk_ur64;
-    case 2:
-    case 3:
     case 8:
     case 9: return tl_ir_walk(ctx, kernel);
     default: return nullptr;

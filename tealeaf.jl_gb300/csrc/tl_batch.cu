@@ -186,13 +186,14 @@ __device__ __forceinline__ void walk_deck32(const DeckDesc &D, const Op &op, int
   }
 }
 
-// FP32 W step of every deck in its inner loop: p' = beta p + r, w = A p', p'.w.
+// FP32 direction step of every deck in its inner loop: p' = beta p + r,
+// p'.A p', p' stored.
 __global__ void __launch_bounds__(256) k_batch_ir_w(const DeckDesc *decks, const BatchMap *map, int parity) {
   const int d = find_deck(map->first_w, map->nblk_w, map->n, blockIdx.x);
   if (d < 0) return;
   const DeckDesc &D = decks[d];
   if (D.F.sc->done) return;
-  OpIrW op;
+  OpIrDir<2> op;
   op.F = D.F;
   op.g = D.g32;
   op.q = D.q;
@@ -205,27 +206,32 @@ __global__ void __launch_bounds__(256) k_batch_ir_w(const DeckDesc *decks, const
   finish_deck<1>(acc, op, nb, lb);
 }
 
-// The FP32 u/r step's epilogue, plus where the search direction ended: after
-// the even step it is in the second buffer.
-struct OpIrURBatch : OpIrUR {
+// The FP32 update step's epilogue, plus where the search direction ended:
+// after the even step it is in the second buffer.
+struct OpIrUpdateBatch : OpIrUpdate<1> {
   int parity;
   __device__ void fin(const double *tot) const {
-    OpIrUR::fin(tot);
+    OpIrUpdate<1>::fin(tot);
     if (F.sc->done) F.sc->pbuf = parity == 0 ? 1 : 0;
   }
 };
 
-// FP32 UR step: x += alpha p', r -= alpha w, r.r, beta, and the refinement test.
+// FP32 update step: A p' recomputed, x += alpha p', r -= alpha A p', r.r,
+// beta, and the refinement test.
 __global__ void __launch_bounds__(256) k_batch_ir_ur(const DeckDesc *decks, const BatchMap *map, int parity) {
   const int d = find_deck(map->first_u, map->nblk_u, map->n, blockIdx.x);
   if (d < 0) return;
   const DeckDesc &D = decks[d];
   if (D.F.sc->done) return;
-  OpIrURBatch op;
+  OpIrUpdateBatch op;
   op.F = D.F;
   op.g = D.g32;
-  op.q = D.q;
-  op.p = parity ? D.p32 : D.pb32;
+  op.s = parity ? D.p32 : D.pb32;
+  op.iw = D.q.iw;
+  op.a = D.q.x;
+  op.b = D.q.r;
+  op.out = nullptr;
+  op.pp = 0;
   op.guard = 0;
   op.cond = 0;
   op.set_cond = 0;
@@ -596,7 +602,7 @@ int batch_solve_ir(tl_batch *b, const double *rx, const double *ry, const tl_par
       snprintf(b->msg, sizeof b->msg, "deck %d: not initialised, or maxiters beyond its tables", k);
       return TL_ERR_STATE;
     }
-    const int rc = tl_ensure_ir(ctx);
+    const int rc = tl_ensure_ir(ctx, 0);  // the batch walks its own tiles: no single-deck tuning
     if (rc) {
       snprintf(b->msg, sizeof b->msg, "deck %d: %s", k, ctx->msg);
       return rc;
@@ -612,11 +618,9 @@ int batch_solve_ir(tl_batch *b, const double *rx, const double *ry, const tl_par
       D.g32.X = ctx->g.X;
       D.g32.Y = ctx->g.Y;
       D.g32.pitch = ctx->ir->pitch;
-      D.q.kx = ctx->ir->kx;
-      D.q.ky = ctx->ir->ky;
       D.q.r = ctx->ir->r;
-      D.q.w = ctx->ir->w;
       D.q.x = ctx->ir->x;
+      D.q.iw = ctx->ir->iw;
       D.p32 = ctx->ir->p;
       D.pb32 = ctx->ir->pb;
       D.ntx32 = (ctx->g.nx + 127) / 128;
@@ -649,8 +653,9 @@ int batch_solve_ir(tl_batch *b, const double *rx, const double *ry, const tl_par
     if (!rc) rc = tl_halo_update(ctx, 1, up, 2, 1);
     if (!rc) rc = tl_copy_u(ctx);
     if (!rc) {
-      k_ir_convert<<<grid_cells_of(ctx->g, 1), 256, 0, b->stream>>>(ctx->F, ctx->g, D.g32, D.q.kx, D.q.ky, D.q.r,
-                                                                    D.p32, D.q.x);
+      k_ir_convert<<<grid_cells_of(ctx->g, 1), 256, 0, b->stream>>>(ctx->F, ctx->g, D.g32, D.q.r, D.p32, D.q.x);
+      k_ir_convert_iw<<<grid_cells_of(ctx->g, 1), 256, 0, b->stream>>>(ctx->F, ctx->g, D.g32, D.q.iw, p.coefficient,
+                                                                       rx[k], ry[k]);
       k_batch_ir_start<<<1, 1, 0, b->stream>>>(ctx->F.sc, IR_DELTA * IR_DELTA);
       if (cudaGetLastError() != cudaSuccess) rc = TL_ERR_CUDA;
     }

@@ -34,32 +34,6 @@ int grid_for(long long n) {
   return (int)(b < 1 ? 1 : b);
 }
 
-void launch_ir_w(tl_ctx *ctx, const float *psrc, float *pdst, int guard, const Walk *walk = nullptr) {
-  OpIrW op;
-  op.F = ctx->F;
-  op.g = g32_of(ctx);
-  op.q = ptrs_of(ctx);
-  op.psrc = psrc;
-  op.pdst = pdst;
-  op.guard = guard;
-  const Walk &wk = walk ? *walk : ctx->ir->walk_w;
-  k_walk32<OpIrW><<<wk.blocks, 32 * wk.warps, 0, ctx->stream>>>(op, wk, ctx->g.ny);
-}
-
-void launch_ir_ur(tl_ctx *ctx, const float *p, int guard, cudaGraphConditionalHandle cond, int set_cond,
-                  const Walk *walk = nullptr) {
-  OpIrUR op;
-  op.F = ctx->F;
-  op.g = g32_of(ctx);
-  op.q = ptrs_of(ctx);
-  op.p = p;
-  op.guard = guard;
-  op.cond = cond;
-  op.set_cond = set_cond;
-  const Walk &wk = walk ? *walk : ctx->ir->walk_ur;
-  k_walk32<OpIrUR><<<wk.blocks, 32 * wk.warps, 0, ctx->stream>>>(op, wk, ctx->g.ny);
-}
-
 template <int AHEAD>
 void launch_ir_dir_t(tl_ctx *ctx, const float *psrc, float *pdst, int guard, const Walk &wk) {
   OpIrDir<AHEAD> op;
@@ -148,8 +122,8 @@ template <int KIND>
 void tune_kind(tl_ctx *ctx, bool tuning) {
   using O2 = OpIrSweep<2, KIND>;
   using O1 = OpIrSweep<1, KIND>;
-  const Walk w2 = tl_autotune(ctx, 128, occupancy_of<O2>(128), occupancy_of<O2>(256), tune_sweep<2, KIND>);
-  const Walk w1 = tl_autotune(ctx, 128, occupancy_of<O1>(128), occupancy_of<O1>(256), tune_sweep<1, KIND>);
+  const Walk w2 = tl_autotune(ctx, 128, occupancy_of<O2>(128), occupancy_of<O2>(256), tuning ? tune_sweep<2, KIND> : nullptr);
+  const Walk w1 = tl_autotune(ctx, 128, occupancy_of<O1>(128), occupancy_of<O1>(256), tuning ? tune_sweep<1, KIND> : nullptr);
   const float t2 = tuning ? time_form(ctx, tune_sweep<2, KIND>, w2, 5) : 1.f;
   const float t1 = tuning ? time_form(ctx, tune_sweep<1, KIND>, w1, 5) : 0.f;
   const int ahead = (t1 >= 0.f && t2 >= 0.f && t2 < t1) ? 2 : 1;
@@ -157,9 +131,12 @@ void tune_kind(tl_ctx *ctx, bool tuning) {
   ctx->ir->walk_sweep[KIND] = ahead == 1 ? w1 : w2;
 }
 
-constexpr int NBUF = 10;  // FP32 arrays: kx, ky, p, pb, r, w, x, sd, sdb, iw
+constexpr int NBUF = 7;  // FP32 arrays: p, pb, r, x, sd, sdb, iw
 
-int ensure_ir(tl_ctx *ctx) {
+// The FP32 buffers of a context, allocated on first use; `tune` autotunes
+// the single-deck kernels' layouts (the batched solve has its own walk and
+// skips it).
+int ensure_ir(tl_ctx *ctx, bool tune = true) {
   if (ctx->ir) return TL_OK;
   tl_ir_state *ir = new (std::nothrow) tl_ir_state();
   if (!ir) return TL_ERR_NOMEM;
@@ -172,17 +149,18 @@ int ensure_ir(tl_ctx *ctx) {
   CK(cudaMemsetAsync(ir->buf, 0, sizeof(float) * ir->stride * NBUF, ctx->stream));
   float *f[NBUF];
   for (int k = 0; k < NBUF; ++k) f[k] = ir->buf + ir->stride * k + ir->lead;
-  ir->kx = f[0]; ir->ky = f[1]; ir->p = f[2]; ir->pb = f[3]; ir->r = f[4]; ir->w = f[5]; ir->x = f[6];
-  ir->sd = f[7]; ir->sdb = f[8]; ir->iw = f[9];
+  ir->p = f[0]; ir->pb = f[1]; ir->r = f[2]; ir->x = f[3]; ir->sd = f[4]; ir->sdb = f[5]; ir->iw = f[6];
   // tune on the zeroed buffers, then zero them again: the trial launches
   // leave NaN behind (alpha = 0/0)
   // OpIrDir and each sweep kind: both forms tuned, the faster kept (without
   // tuning, TEALEAF_GB300_TUNE=0: the fixed layout, the direction step with
   // rows two ahead and the sweeps with rows as reached)
-  const char *tune = getenv("TEALEAF_GB300_TUNE");
-  const bool tuning = !(tune && !strcmp(tune, "0"));
-  const Walk d2 = tl_autotune(ctx, 128, occupancy_of<OpIrDir<2>>(128), occupancy_of<OpIrDir<2>>(256), tune_dir2);
-  const Walk d1 = tl_autotune(ctx, 128, occupancy_of<OpIrDir<1>>(128), occupancy_of<OpIrDir<1>>(256), tune_dir1);
+  const char *env = getenv("TEALEAF_GB300_TUNE");
+  const bool tuning = tune && !(env && !strcmp(env, "0"));
+  const Walk d2 = tl_autotune(ctx, 128, occupancy_of<OpIrDir<2>>(128), occupancy_of<OpIrDir<2>>(256),
+                              tuning ? tune_dir2 : nullptr);
+  const Walk d1 = tl_autotune(ctx, 128, occupancy_of<OpIrDir<1>>(128), occupancy_of<OpIrDir<1>>(256),
+                              tuning ? tune_dir1 : nullptr);
   const float s2 = tuning ? time_form(ctx, tune_dir2, d2, 5) : 0.f;
   const float s1 = tuning ? time_form(ctx, tune_dir1, d1, 5) : 1.f;
   ir->dir_ahead = (s1 >= 0.f && s2 >= 0.f && s1 < s2) ? 1 : 2;
@@ -191,9 +169,6 @@ int ensure_ir(tl_ctx *ctx) {
   tune_kind<SWEEP_PPCG_UPDATE>(ctx, tuning);
   tune_kind<SWEEP_CHEBY>(ctx, tuning);
   tune_kind<SWEEP_PPCG_INNER>(ctx, tuning);
-  // the 48-byte pair (kept for comparison in tl_bench_kernel) on the same layouts
-  ir->walk_w = ir->walk_dir;
-  ir->walk_ur = ir->walk_sweep[SWEEP_CG];
   cudaGetLastError();
   CK(cudaMemsetAsync(ir->buf, 0, sizeof(float) * ir->stride * NBUF, ctx->stream));
   return TL_OK;
@@ -253,7 +228,7 @@ int ir_graph(tl_ctx *ctx, int which, cudaGraphExec_t *out) {
 
 }  // namespace
 
-int tl_ensure_ir(tl_ctx *ctx) { return ensure_ir(ctx); }
+int tl_ensure_ir(tl_ctx *ctx, int tune) { return ensure_ir(ctx, tune != 0); }
 
 void tl_release_ir_graphs(tl_ctx *ctx) {
   if (!ctx->ir) return;
@@ -311,8 +286,8 @@ static int ir_loop(tl_ctx *ctx, const tl_params &p, double rx, double ry, double
                    int *refinements) {
   const G32 g32 = g32_of(ctx);
   tl_ir_state *ir = ctx->ir;
-  k_ir_convert<<<grid_for((long long)ctx->g.X * ctx->g.Y), 256, 0, ctx->stream>>>(ctx->F, ctx->g, g32, ir->kx, ir->ky,
-                                                                                  ir->r, ir->p, ir->x);
+  k_ir_convert<<<grid_for((long long)ctx->g.X * ctx->g.Y), 256, 0, ctx->stream>>>(ctx->F, ctx->g, g32, ir->r, ir->p,
+                                                                                  ir->x);
   k_ir_convert_iw<<<grid_for((long long)ctx->g.X * ctx->g.Y), 256, 0, ctx->stream>>>(ctx->F, ctx->g, g32, ir->iw,
                                                                                      p.coefficient, rx, ry);
   CKL();
@@ -436,8 +411,6 @@ int tl_ir_presteps(tl_ctx *ctx, double rx, double ry, const tl_params *prm, int 
 tl::Walk *tl_ir_walk(tl_ctx *ctx, int kernel) {
   if (ensure_ir(ctx)) return nullptr;
   switch (kernel) {
-    case 2: return &ctx->ir->walk_w;
-    case 3: return &ctx->ir->walk_ur;
     case 8: return &ctx->ir->walk_dir;
     case 9: return &ctx->ir->walk_sweep[SWEEP_CG];
     default: return nullptr;
@@ -696,18 +669,16 @@ int tl_ppcg32_run(tl_ctx *ctx, const tl_params *prm, double rr, int *refinements
 }
 
 // Back-to-back launches of one FP32 kernel on the current FP32 fields (ids as
-// in tl_bench_kernel): 2 OpIrW, 3 OpIrUR, 6 the Chebyshev step, 7 a PPCG
-// inner sweep, 8 OpIrDir, 9 OpIrUpdate.
+// in tl_bench_kernel): 6 the Chebyshev step, 7 a PPCG inner sweep, 8 OpIrDir,
+// 9 the CG update step.
 int tl_ir_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch) {
   int rc = ensure_ir(ctx);
   if (rc) return rc;
-  if (kernel != 2 && kernel != 3 && (kernel < 6 || kernel > 9)) return TL_ERR_ARG;
+  if (kernel < 6 || kernel > 9) return TL_ERR_ARG;
   tl_ir_state *ir = ctx->ir;
   CK(cudaEventRecord(ctx->tev0, ctx->stream));
   for (int k = 0; k < reps; ++k) {
-    if (kernel == 2) launch_ir_w(ctx, (k & 1) ? ir->pb : ir->p, (k & 1) ? ir->p : ir->pb, 0);
-    else if (kernel == 3) launch_ir_ur(ctx, ir->pb, 0, 0, 0);
-    else if (kernel == 8) launch_ir_dir(ctx, (k & 1) ? ir->pb : ir->p, (k & 1) ? ir->p : ir->pb, 0);
+    if (kernel == 8) launch_ir_dir(ctx, (k & 1) ? ir->pb : ir->p, (k & 1) ? ir->p : ir->pb, 0);
     else if (kernel == 9) launch_ir_update(ctx, ir->pb, 0, 0, 0);
     else if (kernel == 6) launch_cheby32(ctx, (k & 1) ? ir->pb : ir->x, (k & 1) ? ir->x : ir->pb, 0);
     else launch_ppcg32_inner(ctx, 1 + (k & 1), 0, 0, 0, 0);

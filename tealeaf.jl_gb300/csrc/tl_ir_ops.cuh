@@ -15,10 +15,9 @@
 struct tl_ir_state {
   float *buf = nullptr;
   long long pitch = 0, lead = 0, stride = 0;
-  float *kx = nullptr, *ky = nullptr, *p = nullptr, *pb = nullptr, *r = nullptr, *w = nullptr, *x = nullptr;
+  float *p = nullptr, *pb = nullptr, *r = nullptr, *x = nullptr;
   float *sd = nullptr, *sdb = nullptr;  // PPCG inner sweeps: the update and its second buffer
   float *iw = nullptr;                  // 1 / w (w = rho or 1/rho, CG.jl:57-60), halo included
-  tl::Walk walk_w{}, walk_ur{};    // autotuned layouts of OpIrW, OpIrUR (and the Chebyshev/PPCG sweeps)
   tl::Walk walk_dir{};              // autotuned layout of OpIrDir
   tl::Walk walk_sweep[4]{};         // autotuned layouts of OpIrSweep, by kind (the last inner sweep shares slot 3)
   int dir_ahead = 2;                // the faster OpIrDir form after tuning (its AHEAD)
@@ -43,8 +42,8 @@ struct G32 {
 };
 
 struct IrPtrs {
-  float *kx, *ky, *r, *w, *x;
-  float *iw;  // inverse weights (the CG step pair OpIrDir / OpIrUpdate)
+  float *r, *x;
+  float *iw;  // inverse weights: Kx = rx/2 (iw_l + iw_c), Ky = ry/2 (iw_d + iw_c)
 };
 
 __device__ __forceinline__ float4 ld4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
@@ -71,146 +70,7 @@ __global__ void __launch_bounds__(256) k_walk32(const Op op, const Walk wk, cons
   if (Op::REDUCES) finish_reduction<1>(acc, op);
 }
 
-// W step: p' = beta*p + r (or p on the first step), w = A32 p', p'.w
-struct OpIrW {
-  static constexpr bool REDUCES = true;
-  Fields F;  // scalars, partials, counter
-  G32 g;
-  IrPtrs q;
-  const float *__restrict__ psrc;
-  float *__restrict__ pdst;
-  int guard;
-  __device__ bool skip() const { return guard && F.sc->done; }
-  __device__ void on_skip() const {}
-
-  // Raw loads of one row, issued one row ahead of their use.
-  struct Row {
-    float4 p, r, kx;
-    float ep, er, kxe;  // edge neighbour (lane 0: i0-1, lane 31: i0+4) and kx at i0+4
-  };
-  __device__ __forceinline__ void load_row(Row &o, int i0, int j, bool valid, bool first, int edge_col) const {
-    if (!valid) return;
-    const size_t c = g.at(i0, j);
-    o.p = ld4(psrc + c);
-    if (!first) o.r = ld4(q.r + c);
-    if (edge_col >= 0) {
-      const size_t e = g.at(edge_col, j);
-      o.ep = __ldg(psrc + e);
-      if (!first) o.er = __ldg(q.r + e);
-    }
-  }
-  __device__ __forceinline__ void load_coef(Row &o, int i0, int j, bool valid, bool kx_edge) const {
-    if (!valid) return;
-    const size_t c = g.at(i0, j);
-    o.kx = ld4(q.kx + c);
-    if (kx_edge) o.kxe = __ldg(q.kx + c + 4);
-  }
-
-  __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
-    const int nx = g.nx, ny = g.ny;
-    const int lane = threadIdx.x & 31;
-    const bool valid = i0 < nx;
-    const int ncell = valid ? min(4, nx - i0) : 0;  // cells this lane owns
-    const bool full = ncell == 4;
-    const bool inner = i0 + 4 < nx;                 // the fourth cell has an interior east neighbour
-    const float beta = (float)F.sc->beta;
-    const bool first = F.sc->first != 0;
-    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-    const int edge_col = !valid ? -1 : (lane == 0 && i0 > 0) ? i0 - 1 : (lane == 31 && inner) ? i0 + 4 : -1;
-    const bool kx_edge = full && (!inner || lane == 31);
-    auto pnew = [&](const Row &o) {
-      return first ? o.p
-                   : make_float4(fmaf(beta, o.p.x, o.r.x), fmaf(beta, o.p.y, o.r.y), fmaf(beta, o.p.z, o.r.z),
-                                 fmaf(beta, o.p.w, o.r.w));
-    };
-    auto pnew_edge = [&](const Row &o) { return first ? o.ep : fmaf(beta, o.ep, o.er); };
-
-    Row cur = {}, nxt = {}, tmp = {};
-    load_row(cur, i0, j0, valid, first, edge_col);
-    load_coef(cur, i0, j0, valid, kx_edge);
-    if (j0 > 0) load_row(tmp, i0, j0 - 1, valid, first, -1);
-    if (j0 + 1 < ny) load_row(nxt, i0, j0 + 1, valid, first, edge_col);
-    float4 kyc = valid ? ld4(q.ky + g.at(i0, j0)) : z;
-    float4 kyn = valid ? ld4(q.ky + g.at(i0, j0 + 1)) : z;
-    float4 pc = valid ? pnew(cur) : z;
-    float4 ps = (j0 > 0 && valid) ? pnew(tmp) : pc;
-    for (int j = j0; j < j1; ++j) {
-      Row nn = {};
-      float4 kyn2 = z;
-      if (j + 1 < j1) {
-        if (j + 2 < ny) load_row(nn, i0, j + 2, valid, first, edge_col);
-        load_coef(nxt, i0, j + 1, valid, kx_edge);
-        kyn2 = valid ? ld4(q.ky + g.at(i0, j + 2)) : z;
-      }
-      const float4 pnn = (j + 1 < ny && valid) ? pnew(nxt) : pc;
-      float pw = __shfl_up_sync(FULL, pc.w, 1);
-      float pe = __shfl_down_sync(FULL, pc.x, 1);
-      float kxe = __shfl_down_sync(FULL, cur.kx.x, 1);
-      if (valid) {
-        if (i0 == 0) pw = pc.x;
-        else if (lane == 0) pw = pnew_edge(cur);
-        if (full) {
-          if (!inner) {
-            pe = pc.w;        // reflect at i = nx-1
-            kxe = cur.kxe;    // kx of the halo column
-          } else if (lane == 31) {
-            pe = pnew_edge(cur);
-            kxe = cur.kxe;
-          }
-        }
-        float wv[4];
-        float part = 0.f;  // this lane's four products, summed in FP32 before the FP64 accumulation
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          if (k < ncell) {
-            const float c = comp(pc, k);
-            const float e = (k + 1 < ncell) ? comp(pc, k + 1) : (k == 3 ? pe : c);  // reflect past nx-1
-            const float wl = (k == 0) ? pw : comp(pc, k - 1);
-            const float k1 = (k == 3) ? kxe : comp(cur.kx, k + 1);
-            const float k0 = comp(cur.kx, k);
-            const float n = comp(pnn, k), sv = comp(ps, k);
-            float t = c;
-            t = fmaf(k1, c - e, t);
-            t = fmaf(k0, c - wl, t);
-            t = fmaf(comp(kyn, k), c - n, t);
-            t = fmaf(comp(kyc, k), c - sv, t);
-            wv[k] = t;
-            part = fmaf(t, c, part);
-          } else {
-            wv[k] = 0.f;
-          }
-        }
-        acc[0] += (double)part;
-        const size_t c0 = g.at(i0, j);
-        if (full) {
-          st4(q.w + c0, make_float4(wv[0], wv[1], wv[2], wv[3]));
-          st4(pdst + c0, pc);
-        } else {
-          for (int k = 0; k < ncell; ++k) {
-            q.w[c0 + k] = wv[k];
-            pdst[c0 + k] = comp(pc, k);
-          }
-        }
-      }
-      ps = pc;
-      pc = pnn;
-      kyc = kyn;
-      kyn = kyn2;
-      cur = nxt;
-      nxt = nn;
-    }
-  }
-  __device__ void fin(const double *tot) const {
-    DevScalars *sc = F.sc;
-    sc->pw = tot[0];
-    sc->alpha = sc->rro / sc->pw;
-    // as CG presteps of Chebyshev, the coefficient table for the eigenvalue
-    // estimate (CG.jl:37; 1-based, maxiters + 2 entries)
-    if (sc->switch_rule == 1 && sc->iter < sc->maxiters) F.cgalpha[sc->iter + 1] = sc->alpha;
-  }
-};
-
-// The epilogue of an FP32 CG step (OpIrUR, OpIrUpdate): beta, the iteration
+// The epilogue of an FP32 CG step (OpIrUpdate): beta, the iteration
 // count, the refinement test and, as CG presteps of Chebyshev or PPCG, the
 // coefficient table and the switch test.
 __device__ __forceinline__ void ir_cg_epilogue(const Fields &F, double rrn, cudaGraphConditionalHandle cond,
@@ -238,54 +98,6 @@ __device__ __forceinline__ void ir_cg_epilogue(const Fields &F, double rrn, cuda
   sc->done = done;
   if (set_cond) cudaGraphSetConditional(cond, done ? 0u : 1u);
 }
-
-// UR step: x += alpha p', r -= alpha w, r.r; the epilogue decides whether the
-// next step is another FP32 iteration or a refinement.
-struct OpIrUR {
-  static constexpr bool REDUCES = true;
-  Fields F;
-  G32 g;
-  IrPtrs q;
-  const float *__restrict__ p;
-  int guard;
-  cudaGraphConditionalHandle cond;
-  int set_cond;
-  __device__ bool skip() const { return guard && F.sc->done; }
-  __device__ void on_skip() const {
-    if (set_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0u);
-  }
-  __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
-    if (i0 >= g.nx) return;
-    const int ncell = min(4, g.nx - i0);
-    const float alpha = (float)F.sc->alpha;
-    double a = acc[0];
-    for (int j = j0; j < j1; ++j) {
-      const size_t c = g.at(i0, j);
-      if (ncell == 4) {
-        const float4 pv = ld4(p + c), wv = ld4(q.w + c);
-        float4 xv = ld4(q.x + c), rv = ld4(q.r + c);
-        xv.x = fmaf(alpha, pv.x, xv.x); xv.y = fmaf(alpha, pv.y, xv.y);
-        xv.z = fmaf(alpha, pv.z, xv.z); xv.w = fmaf(alpha, pv.w, xv.w);
-        rv.x = fmaf(-alpha, wv.x, rv.x); rv.y = fmaf(-alpha, wv.y, rv.y);
-        rv.z = fmaf(-alpha, wv.z, rv.z); rv.w = fmaf(-alpha, wv.w, rv.w);
-        a += (double)fmaf(rv.w, rv.w, fmaf(rv.z, rv.z, fmaf(rv.y, rv.y, rv.x * rv.x)));
-        st4(q.x + c, xv);
-        st4(q.r + c, rv);
-      } else {
-        for (int k = 0; k < ncell; ++k) {
-          const float xv = fmaf(alpha, p[c + k], q.x[c + k]);
-          const float rv = fmaf(-alpha, q.w[c + k], q.r[c + k]);
-          q.x[c + k] = xv;
-          q.r[c + k] = rv;
-          a = fma((double)rv, (double)rv, a);
-        }
-      }
-    }
-    acc[0] = a;
-  }
-  __device__ void fin(const double *tot) const { ir_cg_epilogue(F, tot[0], cond, set_cond); }
-};
-
 
 // ---- the 40-byte CG step pair ----------------------------------------------
 // OpIrDir forms p' = beta p + r and p'.A p' and stores p' (reads p, r, iw:
@@ -688,15 +500,13 @@ struct OpIrResid : NoSkip {
   __device__ void fin(const double *tot) const { F.sc->red[0] = tot[0]; }
 };
 
-// FP32 copies of kx, ky (whole arrays, halo included); p32 = r32 = (float) r
-// and x = 0 on the interior.
-__global__ void k_ir_convert(Fields F, Geom g, G32 g32, float *kx, float *ky, float *r, float *p, float *x) {
+// The start of an FP32 CG loop: p32 = r32 = (float) r on the interior (0 in
+// the halo) and x = 0.
+__global__ void k_ir_convert(Fields F, Geom g, G32 g32, float *r, float *p, float *x) {
   const long long n = (long long)g.X * g.Y;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
     const int I = (int)(k % g.X), J = (int)(k / g.X);
     const size_t c = (size_t)I + (size_t)J * g.pitch, c32 = (size_t)I + (size_t)J * g32.pitch;
-    kx[c32] = (float)F.kx[c];
-    ky[c32] = (float)F.ky[c];
     const bool interior = I >= g.hd && I < g.X - g.hd && J >= g.hd && J < g.Y - g.hd;
     const float rv = interior ? (float)F.r[c] : 0.f;
     r[c32] = rv;
@@ -753,10 +563,7 @@ G32 g32_of(tl_ctx *ctx) {
 
 IrPtrs ptrs_of(tl_ctx *ctx) {
   IrPtrs q;
-  q.kx = ctx->ir->kx;
-  q.ky = ctx->ir->ky;
   q.r = ctx->ir->r;
-  q.w = ctx->ir->w;
   q.x = ctx->ir->x;
   q.iw = ctx->ir->iw;
   return q;

@@ -271,7 +271,7 @@ Walk tl_autotune(tl_ctx *ctx, int cols_per_warp, int occ4, int occ8, void (*laun
   // without tuning (TEALEAF_GB300_TUNE=0): 8 warps, 8-row tiles, 3 blocks per SM
   Walk best = walk_fixed(g.nx, g.ny, cols_per_warp, 8, 8, 3 * ctx->sm_count);
   const char *tune = getenv("TEALEAF_GB300_TUNE");
-  if (tune && !strcmp(tune, "0")) return best;
+  if (!launch || (tune && !strcmp(tune, "0"))) return best;  // no launcher: the fixed layout
   float best_ms = -1.f;
   for (int warps = 4; warps <= 8; warps += 4) {
     const int occ = warps == 4 ? occ4 : occ8;

@@ -82,7 +82,7 @@ int tl_cheby_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_r
 int tl_ppcg_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res);
 int tl_jacobi_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res);
 int tl_ir_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_result *res);
-int tl_ensure_ir(tl_ctx *ctx);  // allocates and tunes the FP32 refinement buffers
+int tl_ensure_ir(tl_ctx *ctx, int tune = 1);  // allocates and tunes the FP32 refinement buffers
 // Chebyshev after its first step, in FP32 inside FP64 refinement (tl_ir.cu)
 int tl_cheby32_run(tl_ctx *ctx, const tl_params *prm, int *refinements, double *rel_out);
 int tl_ir_presteps(tl_ctx *ctx, double rx, double ry, const tl_params *prm, int *refinements, double *rr_out,
