@@ -198,21 +198,22 @@ def run_e2e(tl, n, precision, steps, warmup, warm=0):
         pinned[nm].numpy()[...] = chunk.field(nm).T
     fidx = {"energy": 3, "density": 1}
     dptr = C.POINTER(C.c_double)
-    times = []
+    times, results = [], []
     for k in range(warmup + steps):
         chunk.check(lib.tl_synchronize(chunk.ctx))
         chunk.check(lib.tl_timer_start(chunk.ctx))
         for nm in ("energy", "density"):
             chunk.check(lib.tl_upload(chunk.ctx, fidx[nm], C.cast(pinned[nm].data_ptr(), dptr), X))
-        timestep(tl, chunk, s)
+        r = timestep(tl, chunk, s)
         chunk.check(lib.tl_download(chunk.ctx, fidx["energy"], C.cast(out.data_ptr(), dptr), X))
         ms = C.c_double()
         chunk.check(lib.tl_timer_stop(chunk.ctx, C.byref(ms)))
         pinned["energy"].copy_(out)     # the next step starts from this step's result, as diffuse! does
         if k >= warmup:
             times.append(ms.value)
+            results.append(r)
     chunk.close()
-    return statistics.mean(times), 2 * X * Y * 8, X * Y * 8
+    return statistics.mean(times), 2 * X * Y * 8, X * Y * 8, times, results
 
 
 # FP32 CG iteration: the direction step (read p, r, iw; write p': 16 B) and
@@ -358,7 +359,8 @@ def gpu_arm(args):
     hname, hchunk, hres = headline
     roof = kernel_roofline(tl, hchunk, hname)
     hchunk.close()
-    e2e_ms, h2d, d2h = run_e2e(tl, n, VARIANTS[hname][0], args.steps, args.warmup, warm=VARIANTS[hname][1])
+    e2e_ms, h2d, d2h, e2e_times, e2e_res = run_e2e(tl, n, VARIANTS[hname][0], args.steps, args.warmup,
+                                                   warm=VARIANTS[hname][1])
     value = variants[hname]["ms_per_step"]
     line = {"metric": METRIC, "value": value, "unit": "ms", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False, "scaling": "weak",
@@ -369,7 +371,8 @@ def gpu_arm(args):
                                    "timestep (halo, solve, solvefinished)", "n": n, "seed": DECK_SEED,
                        "variant": hname, "l2": "every field (537 MB at 8192^2) is larger than L2; no flush"},
             "clocks": clocks,
-            "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms": e2e_times, "iters": [r.iters for r in e2e_res], "warm": [r.warm for r in e2e_res]},
             # the solve's own launches plus the halo and solvefinished! kernels of each step
             "gpu_launches": int(sum(r.launches for r in hres) + 4 * len(hres)),
             "variants": variants,
