@@ -196,24 +196,42 @@ def run_e2e(tl, n, precision, steps, warmup, warm=0):
     out = torch.empty((Y, X), dtype=torch.float64, pin_memory=True)
     for nm in pinned:
         pinned[nm].numpy()[...] = chunk.field(nm).T
+    # host-side check of the staging buffers: pinned, and a plain copy's rate
+    dev = torch.empty((Y, X), dtype=torch.float64, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dev.copy_(pinned["energy"], non_blocking=True)
+    e0.record()
+    dev.copy_(pinned["energy"], non_blocking=True)
+    e1.record()
+    e1.synchronize()
+    probe = {"pinned": all(t.is_pinned() for t in list(pinned.values()) + [out]),
+             "torch_h2d_gbs": X * Y * 8 / (e0.elapsed_time(e1) * 1e-3) / 1e9}
+    del dev
     fidx = {"energy": 3, "density": 1}
     dptr = C.POINTER(C.c_double)
-    times, results = [], []
+    times, results, phases = [], [], []
     for k in range(warmup + steps):
         chunk.check(lib.tl_synchronize(chunk.ctx))
         chunk.check(lib.tl_timer_start(chunk.ctx))
+        w0 = time.perf_counter()
         for nm in ("energy", "density"):
             chunk.check(lib.tl_upload(chunk.ctx, fidx[nm], C.cast(pinned[nm].data_ptr(), dptr), X))
+        w1 = time.perf_counter()
         r = timestep(tl, chunk, s)
+        chunk.check(lib.tl_synchronize(chunk.ctx))
+        w2 = time.perf_counter()
         chunk.check(lib.tl_download(chunk.ctx, fidx["energy"], C.cast(out.data_ptr(), dptr), X))
+        w3 = time.perf_counter()
         ms = C.c_double()
         chunk.check(lib.tl_timer_stop(chunk.ctx, C.byref(ms)))
         pinned["energy"].copy_(out)     # the next step starts from this step's result, as diffuse! does
         if k >= warmup:
             times.append(ms.value)
             results.append(r)
+            phases.append({"upload": (w1 - w0) * 1e3, "step": (w2 - w1) * 1e3, "download": (w3 - w2) * 1e3})
     chunk.close()
-    return statistics.mean(times), 2 * X * Y * 8, X * Y * 8, times, results
+    phases.append(probe)
+    return statistics.mean(times), 2 * X * Y * 8, X * Y * 8, times, results, phases
 
 
 # FP32 CG iteration: the direction step (read p, r, iw; write p': 16 B) and
@@ -359,8 +377,8 @@ def gpu_arm(args):
     hname, hchunk, hres = headline
     roof = kernel_roofline(tl, hchunk, hname)
     hchunk.close()
-    e2e_ms, h2d, d2h, e2e_times, e2e_res = run_e2e(tl, n, VARIANTS[hname][0], args.steps, args.warmup,
-                                                   warm=VARIANTS[hname][1])
+    e2e_ms, h2d, d2h, e2e_times, e2e_res, e2e_phases = run_e2e(tl, n, VARIANTS[hname][0], args.steps, args.warmup,
+                                                               warm=VARIANTS[hname][1])
     value = variants[hname]["ms_per_step"]
     line = {"metric": METRIC, "value": value, "unit": "ms", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False, "scaling": "weak",
@@ -372,7 +390,8 @@ def gpu_arm(args):
                        "variant": hname, "l2": "every field (537 MB at 8192^2) is larger than L2; no flush"},
             "clocks": clocks,
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "ms": e2e_times, "iters": [r.iters for r in e2e_res], "warm": [r.warm for r in e2e_res]},
+                    "ms": e2e_times, "iters": [r.iters for r in e2e_res], "warm": [r.warm for r in e2e_res],
+                    "host_wall_ms": e2e_phases},
             # the solve's own launches plus the halo and solvefinished! kernels of each step
             "gpu_launches": int(sum(r.launches for r in hres) + 4 * len(hres)),
             "variants": variants,

@@ -175,26 +175,58 @@ static int check_field(tl_ctx *ctx, int field, int ld) {
   return TL_OK;
 }
 
+// Pinned (page-locked, mapped) host memory is read and written by a kernel
+// over the host link; any other host memory goes through cudaMemcpy2DAsync.
+// On this part the kernel path runs at the link's rate, as the copy engines
+// do, and keeps that rate where the copy engines' slows down under sustained
+// load.
+static const void *mapped_ptr(const void *host) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+__global__ void k_copy_pitched(double *__restrict__ dst, long long dpitch, const double *__restrict__ src,
+                               long long spitch, int X, int Y) {
+  const long long n = (long long)X * Y;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const long long i = k % X, j = k / X;
+    dst[i + j * dpitch] = src[i + j * spitch];
+  }
+}
+
+static int copy_field(tl_ctx *ctx, double *dst, long long dpitch, const double *src, long long spitch,
+                      cudaMemcpyKind kind, const void *host) {
+  const Geom &g = ctx->g;
+  const void *mapped = mapped_ptr(host);
+  if (mapped) {
+    const double *s = kind == cudaMemcpyHostToDevice ? static_cast<const double *>(mapped) : src;
+    double *d = kind == cudaMemcpyHostToDevice ? dst : static_cast<double *>(const_cast<void *>(mapped));
+    k_copy_pitched<<<8 * ctx->sm_count, 256, 0, ctx->stream>>>(d, dpitch, s, spitch, g.X, g.Y);
+    CKL();
+  } else {
+    CK(cudaMemcpy2DAsync(dst, sizeof(double) * dpitch, src, sizeof(double) * spitch, sizeof(double) * g.X, g.Y,
+                         kind, ctx->stream));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return TL_OK;
+}
+
 extern "C" int tl_upload(tl_ctx *ctx, int field, const double *host, int ld) {
   if (!ctx || !host) return TL_ERR_ARG;
   int rc = check_field(ctx, field, ld);
   if (rc) return rc;
-  const Geom &g = ctx->g;
-  CK(cudaMemcpy2DAsync(ctx->field_ptr[field], sizeof(double) * g.pitch, host, sizeof(double) * ld,
-                       sizeof(double) * g.X, g.Y, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  return TL_OK;
+  return copy_field(ctx, ctx->field_ptr[field], ctx->g.pitch, host, ld, cudaMemcpyHostToDevice, host);
 }
 
 extern "C" int tl_download(tl_ctx *ctx, int field, double *host, int ld) {
   if (!ctx || !host) return TL_ERR_ARG;
   int rc = check_field(ctx, field, ld);
   if (rc) return rc;
-  const Geom &g = ctx->g;
-  CK(cudaMemcpy2DAsync(host, sizeof(double) * ld, ctx->field_ptr[field], sizeof(double) * g.pitch,
-                       sizeof(double) * g.X, g.Y, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  return TL_OK;
+  return copy_field(ctx, host, ld, ctx->field_ptr[field], ctx->g.pitch, cudaMemcpyDeviceToHost, host);
 }
 
 // ---------------------------------------------------------------------------

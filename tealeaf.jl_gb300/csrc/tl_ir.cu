@@ -1,9 +1,10 @@
 // tl_ir.cu -- CG with FP32 inner sweeps inside FP64 refinement.
 //
-// The inner iteration is CG on FP32 vectors (p, r, w and the correction x)
-// with FP32 Kx/Ky; each dot sums a lane's four products in FP32 and
-// accumulates those partial sums in FP64 (one FP64 add per four cells: the
-// FP64 pipe of this part issues 1/64 as fast as FP32).  Whenever the FP32 residual has dropped by a factor
+// The inner iteration is CG on FP32 vectors (p, r and the correction x) with
+// the stencil faces formed from FP32 inverse weights; each dot sums a lane's
+// products over eight rows in FP32 and accumulates those partial sums in
+// FP64 (one FP64 add per 32 cells: the FP64 pipe of this part issues 1/64 as
+// fast as FP32).  Whenever the FP32 residual has dropped by a factor
 // delta since the last refinement, or claims convergence, the loop returns to
 // a refinement step done entirely in FP64:
 //     u += x;  x = 0;  r = u0 - A u (true residual);  test ||r|| / ||u0||.
@@ -15,7 +16,8 @@
 // interior cell of each row 128-byte aligned; each lane owns 4 consecutive
 // cells (one float4).  The FP32 stencil uses the difference form
 // w = p + kx1 (p - pE) + kx0 (p - pW) + ky1 (p - pN) + ky0 (p - pS), which
-// keeps the identity term exact where the large coupling terms cancel.
+// keeps the identity term exact where the large coupling terms cancel, with
+// kx = rx/2 (iw_W + iw) and ky = ry/2 (iw_S + iw) from the inverse weights.
 #include <cmath>
 #include <cstdlib>
 #include <cstring>

@@ -2,9 +2,10 @@
 // their FP64 refinement steps, shared by the single-deck solve (tl_ir.cu) and
 // the batched solve (tl_batch.cu).
 //
-// The inner iteration is CG on FP32 vectors (p, r, w and the correction x)
-// with FP32 Kx/Ky; each dot sums a lane's four products in FP32 and
-// accumulates those partial sums in FP64.  FP32 arrays are pitched like the
+// The inner iteration is CG on FP32 vectors (p, r and the correction x) with
+// the stencil faces formed from FP32 inverse weights; each dot sums a lane's
+// products over eight rows (32 cells) in FP32 and accumulates those partial
+// sums in FP64.  FP32 arrays are pitched like the
 // FP64 fields, 32 floats per pitch unit, first interior cell of each row
 // 128-byte aligned; each lane owns 4 consecutive cells (one float4).
 #pragma once
@@ -213,6 +214,8 @@ struct OpIrDir {
     float4 pc = valid ? pnew(cur) : z;
     float4 ps = (j0 > 0 && valid) ? pnew(sth) : pc;
     float4 is = (j0 > 0 && valid) ? sth.iw : cur.iw;
+    float fpart = 0.f;
+    int nrow = 0;
     for (int j = j0; j < j1; ++j) {
       Row nn = {};
       if (AHEAD == 2) {
@@ -237,7 +240,12 @@ struct OpIrDir {
 #pragma unroll
         for (int k = 0; k < 4; ++k)
           if (k < ncell) part = fmaf(wv[k], comp(pc, k), part);
-        acc[0] += (double)part;
+        fpart += part;
+        if (++nrow == 8) {  // eight rows of FP32 partials (32 products) per FP64 add
+          acc[0] += (double)fpart;
+          fpart = 0.f;
+          nrow = 0;
+        }
         const size_t c0 = g.at(i0, j);
         if (full) {
           st4(pdst + c0, pc);
@@ -253,6 +261,7 @@ struct OpIrDir {
       cur = nxt;
       if (AHEAD == 2) nxt = nn;
     }
+    acc[0] += (double)fpart;
   }
   __device__ void fin(const double *tot) const {
     DevScalars *sc = F.sc;
@@ -351,6 +360,8 @@ struct OpIrSweep {
     float4 is = (j0 > 0 && valid) ? ld(iw, j0 - 1) : cur.iw;
     if (AHEAD == 2 && j0 + 1 < ny) load_nb(nxt, i0, j0 + 1, valid, lane, inner);
     double racc = acc[0];
+    float fpart = 0.f;
+    int nrow = 0;
     for (int j = j0; j < j1; ++j) {
       Nb nn = {};
       if (AHEAD == 2) {
@@ -397,7 +408,14 @@ struct OpIrSweep {
           }
           if (REDUCES && k < ncell) part = fmaf(rr, rr, part);
         }
-        if (REDUCES) racc += (double)part;
+        if (REDUCES) {
+          fpart += part;
+          if (++nrow == 8) {  // eight rows of FP32 partials (32 products) per FP64 add
+            racc += (double)fpart;
+            fpart = 0.f;
+            nrow = 0;
+          }
+        }
         const size_t o = g.at(i0, j);
         const bool st_a = KIND != SWEEP_CHEBY, st_o = KIND != SWEEP_CG;
         if (full) {
@@ -421,6 +439,7 @@ struct OpIrSweep {
       ac = an;
       bc = bn;
     }
+    if (REDUCES) racc += (double)fpart;
     acc[0] = racc;
   }
   __device__ void fin(const double *tot) const {

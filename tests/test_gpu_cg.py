@@ -230,3 +230,36 @@ def test_c_driver_matches_host_mirror(tl, built_lib, tmp_path, mode, precision, 
         assert all(abs(a - b) <= max(3, 0.05 * b) for a, b in zip(iters, [r.iters for r in steps]))
         for x, y in zip(sums[-1], hsums[-1]):
             assert rel(x, y) <= 1e-9
+
+
+@pytest.mark.parametrize("ld_extra", [0, 3])
+def test_upload_download_pinned_and_pageable(tl, built_lib, ld_extra):
+    """tl_upload / tl_download move the same bits through both paths: pinned
+    (mapped) host memory, copied by a kernel over the host link, and pageable
+    memory, copied by cudaMemcpy2DAsync; with a leading dimension equal to X
+    and larger than X."""
+    import ctypes as C
+    import torch
+    s = tl.Settings.from_text(random_deck(37, 5, ny=29, steps=1), mode=TEA)
+    chunk = tl.initialiseapp(s)
+    X, Y = chunk.size()
+    ld = X + ld_extra
+    rng = np.random.default_rng(ld_extra)
+    src = rng.standard_normal((Y, ld))
+    dptr = C.POINTER(C.c_double)
+    lib, ctx = chunk.lib, chunk.ctx
+    k = tl._abi.FIELDS.index("sd")
+    pinned = torch.from_numpy(src.copy()).pin_memory()
+    back_pinned = torch.zeros((Y, ld), dtype=torch.float64).pin_memory()
+    back_pageable = np.zeros((Y, ld))
+    chunk.check(lib.tl_upload(ctx, k, C.cast(pinned.data_ptr(), dptr), ld))
+    chunk.check(lib.tl_download(ctx, k, C.cast(back_pinned.data_ptr(), dptr), ld))
+    chunk.check(lib.tl_download(ctx, k, back_pageable.ctypes.data_as(dptr), ld))
+    np.testing.assert_array_equal(back_pinned.numpy()[:, :X], src[:, :X])
+    np.testing.assert_array_equal(back_pageable[:, :X], src[:, :X])
+    assert not back_pinned.numpy()[:, X:].any() and not back_pageable[:, X:].any()  # columns past X untouched
+    pageable = np.ascontiguousarray(src[::-1])
+    chunk.check(lib.tl_upload(ctx, k, pageable.ctypes.data_as(dptr), ld))
+    chunk.check(lib.tl_download(ctx, k, C.cast(back_pinned.data_ptr(), dptr), ld))
+    np.testing.assert_array_equal(back_pinned.numpy()[:, :X], pageable[:, :X])
+    chunk.close()

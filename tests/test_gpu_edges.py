@@ -87,3 +87,21 @@ def test_fp32_refined_tiny_decks(tl, built_lib, nx, ny):
     assert all(r.converged and r.rel_residual < 1e-10 for r in r32)
     u32, u64 = p32[-1]["u"], p64[-1]["u"]
     assert np.max(np.abs(u32 - u64)) <= 1e-8 * max(np.max(np.abs(u64)), 1e-300)
+
+
+@pytest.mark.parametrize("solver", ["cg", "cheby", "ppcg"])
+@pytest.mark.parametrize("nx,ny,hd", [(2, 40, 2), (3, 33, 1), (6, 17, 3), (7, 129, 1), (131, 9, 4)])
+def test_fp32_sweeps_ragged_widths_and_halo_depths(tl, built_lib, solver, nx, ny, hd):
+    """Every FP32 sweep kernel on widths that leave a lane with 2, 3 or 1
+    cells (and a ragged last warp strip at 131), with halo depths 1, 3 and 4:
+    the 1e-10 relative true residual is met and u matches FP64 on the
+    interior.  Cheby and PPCG switch after 5 CG presteps, so the Chebyshev
+    and PPCG sweeps run."""
+    text = random_deck(nx, 21, ny=ny, nrect=3, steps=2, eps=1e-10, solver=solver, halo_depth=hd, presteps=5,
+                       ppcg_inner_steps=4)
+    _, r32, _, p32 = gpu_run(tl, text, TEA, steps_fields=True, criterion=1, precision=1)
+    _, r64, _, p64 = gpu_run(tl, text, TEA, steps_fields=True, criterion=1, precision=0)
+    assert all(r.converged and 0 <= r.rel_residual < 1e-10 for r in r32), r32
+    assert all(r.converged for r in r64)
+    u32, u64 = p32[-1]["u"][hd:-hd, hd:-hd], p64[-1]["u"][hd:-hd, hd:-hd]
+    assert np.max(np.abs(u32 - u64)) <= 1e-8 * np.max(np.abs(u64))
