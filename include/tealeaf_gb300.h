@@ -301,9 +301,15 @@ typedef struct {
  * mode 0: out = y; 1: out = GELU(y) and z = y (z may be NULL); 2: out = y *
  * GELU'(gz) (input gradient through the previous layer's GELU; b may be NULL).
  * out32 (may be NULL) receives channel 0 of y in FP32.  (cin, cout) in
- * {(16, 32), (32, 32), (32, 16)}. */
+ * {(16, 32), (32, 32), (32, 16)}.  Runs on the tcgen05 tensor cores
+ * (TEALEAF_GB300_CONV=mma selects the warp-level mma.sync kernel). */
 int tl_conv3x3_forward(const void *x, const void *w, const float *bias, const void *gz, void *z, void *out,
                        float *out32, int N, int H, int W, int cin, int cout, int mode, void *stream);
+/* Synchronises the device, then returns in *timeouts the number of blocks of
+ * the tcgen05 convolution whose bounded wait for their MMAs ran out since the
+ * last call (0 in a correct run; such a block stops and leaves its rows
+ * unwritten), and resets the count. */
+int tl_conv_status(int *timeouts);
 /* dw[cout][9][cin], then db[cout] = the weight and bias gradients; partials
  * holds nparts * (cout*9*cin + cout) floats. */
 int tl_conv3x3_weight_grad(const void *x, const void *dz, float *partials, int nparts, float *dw, int N, int H, int W,

@@ -114,6 +114,7 @@ SIGNATURES = {
     "tl_conv3x3_weight_grad": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int,
                                 C.c_int, C.c_int, C.c_void_p], C.c_int),
     "tl_conv3x3_flip": ([C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p], C.c_int),
+    "tl_conv_status": ([C.POINTER(C.c_int)], C.c_int),
     "tl_adam_step": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_float,
                       C.c_float, C.c_float, C.c_int, C.c_float, C.c_float, C.c_void_p], C.c_int),
     "tl_warm_features": ([C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p], C.c_int),

@@ -12,6 +12,8 @@
 
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
+#include <cstring>
 
 #include "tl_conv.h"
 
@@ -218,6 +220,281 @@ __global__ void __launch_bounds__(128) k_conv3x3(ConvArgs a) {
     __syncthreads();
   }
 }
+
+// ---------------------------------------------------------------------------
+// The same convolution on the 5th-generation tensor cores (tcgen05)
+// ---------------------------------------------------------------------------
+//
+// One block computes FTP = 128 pixels of an image row per step, FRB rows in
+// turn, as a GEMM with M = 128 pixels, N = COUT, K = 9 taps x CIN: one
+// tcgen05.mma (M 128, N COUT, K 16, BF16 in, FP32 accumulate) per tap and
+// 16-channel step, issued by one thread, accumulating in tensor memory.
+// Operands are read by the tensor core straight from shared memory through
+// matrix descriptors in the no-swizzle K-major layout, whose unit is an 8 x 8
+// BF16 core matrix of eight 16-byte rows:
+//   input row:  [CIN/8 channel chunks][FTP + 2 pixels][8 channels]; the core
+//               matrices of a chunk are 128 B apart along the pixels (SBO) and
+//               the chunks (FTP + 2) x 16 B apart (LBO, the K direction), so
+//               the A operand of tap (dy, dx) is the staged row y - 1 + dy
+//               shifted by dx pixels: a descriptor, no im2col copy;
+//   weights:    [9 CIN/8 k chunks][COUT][8 k values]; core matrices 128 B apart
+//               along the output channels (SBO), k chunks COUT x 16 B apart (LBO).
+// Input rows live in a four-slot ring filled by cp.async (row y + 2 is
+// fetched while row y is computed).  The MMAs of a row complete on an
+// mbarrier (tcgen05.commit); every thread then reads its pixel's COUT
+// accumulators from its warp's tensor-memory lane quadrant (tcgen05.ld) for
+// the epilogue.  Every mbarrier wait is bounded: a wait that runs out stops
+// the block and counts in g_conv_timeouts.
+namespace tc {
+
+__device__ int g_conv_timeouts;
+
+// GELU and its derivative with the hardware tanh (tanh.approx.f32, relative
+// error about 2^-11, below the BF16 rounding of the outputs).
+__device__ __forceinline__ float tanh_hw(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;\n" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float gelu_hw(float z) {
+  const float c = 0.7978845608028654f;
+  return 0.5f * z * (1.f + tanh_hw(c * (z + 0.044715f * z * z * z)));
+}
+__device__ __forceinline__ float gelu_grad_hw(float z) {
+  const float c = 0.7978845608028654f;
+  const float t = tanh_hw(c * (z + 0.044715f * z * z * z));
+  return 0.5f * (1.f + t) + 0.5f * z * (1.f - t * t) * c * (1.f + 3.f * 0.044715f * z * z);
+}
+constexpr int SPIN_LIMIT = 1 << 22;
+constexpr int TCOLS = 32;  // tensor-memory columns of one accumulator buffer (COUT <= 32); two per block
+
+__device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor: no swizzle, start, leading (K) and stride
+// (M/N) byte offsets, descriptor version 1.
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+
+// Instruction descriptor of kind::f16: F32 accumulator, BF16 A and B, both
+// K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(id), "r"(acc));
+}
+__device__ __forceinline__ void commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(saddr(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool bar_try(uint64_t *bar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(saddr(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+// 16 consecutive FP32 accumulator columns of this thread's lane.
+__device__ __forceinline__ void tld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+template <int CIN, int COUT>
+struct Smem {
+  static constexpr int NC = CIN / 8;             // channel chunks of an input pixel
+  static constexpr int ROWB = (FTP + 2) * 16;    // bytes of one chunk of a staged row
+  static constexpr int SLOT = NC * ROWB;         // bytes of one staged input row
+  static constexpr int KC = 9 * CIN / 8;         // k chunks of the weights
+  static constexpr int WB = KC * COUT * 16;      // bytes of the weights
+  static constexpr int BIAS = WB + 4 * SLOT;     // COUT floats
+  static constexpr int BAR = BIAS + 4 * COUT;    // two mbarriers and the tensor-memory address
+  static constexpr int BYTES = BAR + 32;
+};
+
+// Rows are pipelined: while the epilogue of row y reads its accumulators
+// from one tensor-memory buffer, the MMAs of row y + 1 run into the other.
+template <int CIN, int COUT, int MODE>
+__global__ void __launch_bounds__(128) k_conv3x3_tc(ConvArgs a) {
+  using S = Smem<CIN, COUT>;
+  static_assert(COUT % 16 == 0 && COUT <= TCOLS && CIN % 16 == 0, "tile shape");
+  constexpr uint32_t ID = idesc(128, COUT);
+  extern __shared__ __align__(128) unsigned char smem[];
+  unsigned char *sw = smem;
+  unsigned char *sx = smem + S::WB;
+  float *sbias = reinterpret_cast<float *>(smem + S::BIAS);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + S::BAR);  // bar[0], bar[1]
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 2);
+  const int img = blockIdx.z, x0 = blockIdx.x * FTP, y0 = blockIdx.y * FRB;
+  const int y1 = min(a.H, y0 + FRB);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const size_t plane = (size_t)a.H * a.W;
+  const bf16 *xi = a.x + (size_t)img * plane * CIN;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr(tslot)),
+                 "r"(2 * TCOLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(bar)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(bar + 1)));
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (tid < COUT) sbias[tid] = a.bias ? a.bias[tid] : 0.f;
+  for (int v = tid; v < COUT * S::KC; v += 128) {
+    const int co = v / S::KC, kc = v % S::KC;
+    cp_async16(sw + (kc * COUT + co) * 16, a.w + (size_t)co * 9 * CIN + kc * 8, 16);
+  }
+  auto load_row = [&](int yy) {
+    unsigned char *dst = sx + ((yy + 4) & 3) * S::SLOT;
+    for (int v = tid; v < (FTP + 2) * S::NC; v += 128) {
+      const int col = v / S::NC, c8 = v % S::NC, xx = x0 + col - 1;
+      const bool in = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
+      const bf16 *src = in ? xi + ((size_t)yy * a.W + xx) * CIN + c8 * 8 : xi;
+      cp_async16(dst + c8 * S::ROWB + col * 16, src, in ? 16 : 0);
+    }
+  };
+  const uint32_t wbase = saddr(sw), xbase = saddr(sx);
+  // the MMAs of row y into tensor-memory buffer b, completing on bar[b]
+  auto issue = [&](int y, int b, uint32_t tmem) {
+    const uint32_t d = tmem + b * TCOLS;
+#pragma unroll
+    for (int dy = 0; dy < 3; ++dy) {
+      const uint32_t rbase = xbase + ((y - 1 + dy + 4) & 3) * S::SLOT;
+#pragma unroll
+      for (int dx = 0; dx < 3; ++dx) {
+        const int tap = 3 * dy + dx;
+#pragma unroll
+        for (int cc = 0; cc < CIN; cc += 16) {
+          const uint64_t ad = sdesc(rbase + (cc / 8) * S::ROWB + dx * 16, S::ROWB, 128);
+          const uint64_t bd = sdesc(wbase + ((tap * CIN + cc) / 8) * COUT * 16, COUT * 16, 128);
+          mma(d, ad, bd, ID, (tap | cc) != 0);
+        }
+      }
+    }
+    commit(bar + b);
+  };
+  // rows y0 - 1 .. y0 + 2 (row y0 + 2 feeds the MMAs of row y0 + 1)
+  for (int r = -1; r <= 2; ++r)
+    if (y0 + r <= y1) load_row(y0 + r);
+  cp_async_commit();
+  cp_async_wait_all();
+  fence_async_smem();
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = *tslot;
+  if (tid == 0) issue(y0, 0, tmem);
+  uint32_t phases = 0u;  // bit b: the parity of mbarrier b's next completion
+  const int xx = x0 + tid;  // this thread's pixel in the epilogue
+  for (int y = y0; y < y1; ++y) {
+    const int b = (y - y0) & 1;
+    // MODE 2: the epilogue's GELU' inputs, loaded while the MMAs run
+    uint4 gzv[MODE == 2 ? COUT / 8 : 1];
+    if (MODE == 2 && xx < a.W) {
+      const uint4 *gp = reinterpret_cast<const uint4 *>(a.gz + ((size_t)img * plane + (size_t)y * a.W + xx) * COUT);
+#pragma unroll
+      for (int q = 0; q < (MODE == 2 ? COUT / 8 : 1); ++q) gzv[q] = gp[q];
+    }
+    bool done = false;
+    for (int it = 0; it < SPIN_LIMIT && !done; ++it) done = bar_try(bar + b, (phases >> b) & 1u);
+    phases ^= 1u << b;
+    if (__syncthreads_or(!done)) {
+      if (tid == 0) atomicAdd(&g_conv_timeouts, 1);
+      break;
+    }
+    // the MMAs of row y are done: row y - 1's slot takes row y + 3
+    const bool more = y + 3 <= y1;
+    if (more) {
+      load_row(y + 3);
+      cp_async_commit();
+    }
+    if (y + 1 < y1) {
+      // row y + 2 (the group before the newest) must have landed
+      if (more) asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+      else cp_async_wait_all();
+      fence_async_smem();
+      fence_before();
+      __syncthreads();
+      fence_after();
+      if (tid == 0) issue(y + 1, b ^ 1, tmem);
+    }
+    fence_after();
+    float acc[COUT];
+#pragma unroll
+    for (int c = 0; c < COUT; c += 16) {
+      float v[16];
+      tld16(tmem + ((uint32_t)(32 * warp) << 16) + b * TCOLS + c, v);
+#pragma unroll
+      for (int k = 0; k < 16; ++k) acc[c + k] = v[k];
+    }
+    fence_before();
+    if (xx < a.W) {
+      const size_t pix = (size_t)img * plane + (size_t)y * a.W + xx;
+#pragma unroll
+      for (int c = 0; c < COUT; ++c) acc[c] += sbias[c];
+      if (a.out32) a.out32[pix] = acc[0];
+      uint4 zo[COUT / 8], oo[COUT / 8];
+#pragma unroll
+      for (int q = 0; q < COUT / 8; ++q) {
+        __nv_bfloat162 *zp = reinterpret_cast<__nv_bfloat162 *>(&zo[q]);
+        __nv_bfloat162 *op = reinterpret_cast<__nv_bfloat162 *>(&oo[q]);
+        const __nv_bfloat162 *gq = reinterpret_cast<const __nv_bfloat162 *>(&gzv[MODE == 2 ? q : 0]);
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const float z0 = acc[8 * q + 2 * h], z1 = acc[8 * q + 2 * h + 1];
+          float o0 = z0, o1 = z1;
+          if (MODE == 1) {
+            zp[h] = __floats2bfloat162_rn(z0, z1);
+            o0 = gelu_hw(z0);
+            o1 = gelu_hw(z1);
+          } else if (MODE == 2) {
+            o0 = z0 * gelu_grad_hw(__low2float(gq[h]));
+            o1 = z1 * gelu_grad_hw(__high2float(gq[h]));
+          }
+          op[h] = __floats2bfloat162_rn(o0, o1);
+        }
+      }
+      if (MODE == 1 && a.z) {
+        uint4 *zd = reinterpret_cast<uint4 *>(a.z + pix * COUT);
+#pragma unroll
+        for (int q = 0; q < COUT / 8; ++q) zd[q] = zo[q];
+      }
+      if (a.out) {
+        uint4 *od = reinterpret_cast<uint4 *>(a.out + pix * COUT);
+#pragma unroll
+        for (int q = 0; q < COUT / 8; ++q) od[q] = oo[q];
+      }
+    }
+  }
+  cp_async_wait_all();
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(2 * TCOLS));
+}
+
+}  // namespace tc
 
 // Weight and bias gradients: dW[co][tap][ci] = sum_p dz[p][co] x[p + off(tap)][ci]
 // as a GEMM with M = COUT, N = 9*CIN, K = pixels; db[co] = sum_p dz[p][co].
@@ -479,16 +756,36 @@ inline int grid_for(long long n) {
   return (int)(b < 1 ? 1 : b);
 }
 
+// The forward kernel: tcgen05 by default; TEALEAF_GB300_CONV=mma selects the
+// warp-level mma.sync kernel (kept for comparison).
+bool conv_use_mma() {
+  static const int v = [] {
+    const char *e = getenv("TEALEAF_GB300_CONV");
+    return (e && !strcmp(e, "mma")) ? 1 : 0;
+  }();
+  return v != 0;
+}
+
 template <int CIN, int COUT, int MODE>
 void launch_conv_mode(const ConvArgs &a, cudaStream_t st) {
-  constexpr int smem = conv_smem_bytes<CIN, COUT>();
-  static bool attr = false;  // the dynamic shared memory limit, set once per kernel
+  const dim3 grid((a.W + FTP - 1) / FTP, (a.H + FRB - 1) / FRB, a.N);
+  if (conv_use_mma()) {
+    constexpr int smem = conv_smem_bytes<CIN, COUT>();
+    static bool attr = false;  // the dynamic shared memory limit, set once per kernel
+    if (!attr) {
+      cudaFuncSetAttribute(k_conv3x3<CIN, COUT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+      attr = true;
+    }
+    k_conv3x3<CIN, COUT, MODE><<<grid, 128, smem, st>>>(a);
+    return;
+  }
+  constexpr int smem = tc::Smem<CIN, COUT>::BYTES;
+  static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_conv3x3<CIN, COUT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(tc::k_conv3x3_tc<CIN, COUT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     attr = true;
   }
-  const dim3 grid((a.W + FTP - 1) / FTP, (a.H + FRB - 1) / FRB, a.N);
-  k_conv3x3<CIN, COUT, MODE><<<grid, 128, smem, st>>>(a);
+  tc::k_conv3x3_tc<CIN, COUT, MODE><<<grid, 128, smem, st>>>(a);
 }
 
 template <int CIN, int COUT>
@@ -526,6 +823,16 @@ int tl_conv_forward(const void *x, const void *w, const float *bias, const void 
 extern "C" int tl_conv3x3_forward(const void *x, const void *w, const float *bias, const void *gz, void *z, void *out,
                                   float *out32, int N, int H, int W, int cin, int cout, int mode, void *stream) {
   return tl_conv_forward(x, w, bias, gz, z, out, out32, N, H, W, cin, cout, mode, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int tl_conv_status(int *timeouts) {
+  if (!timeouts) return TL_ERR_ARG;
+  if (cudaDeviceSynchronize() != cudaSuccess) return TL_ERR_CUDA;
+  const int zero = 0;
+  if (cudaMemcpyFromSymbol(timeouts, tc::g_conv_timeouts, sizeof(int)) != cudaSuccess ||
+      cudaMemcpyToSymbol(tc::g_conv_timeouts, &zero, sizeof(int)) != cudaSuccess)
+    return TL_ERR_CUDA;
+  return TL_OK;
 }
 
 extern "C" int tl_conv3x3_weight_grad(const void *x, const void *dz, float *partials, int nparts, float *dw, int N,

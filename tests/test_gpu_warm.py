@@ -9,6 +9,8 @@ tanh can move a value across a rounding boundary) plus FP32 accumulation, FP32 o
 at the same points) agrees per layer to 5e-2 in norm: a different FP32
 summation order can flip a BF16 rounding, which then propagates.
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -262,3 +264,5 @@ def test_conv_forward_ragged_shapes(tl, built_lib, cin, cout, mode):
         close_bf16(f64(zd), W.bf16(z), "pre-activation")
     gg = g32.cpu().numpy().astype(np.float64)
     assert np.max(np.abs(gg - z[..., 0])) <= 1e-5 * np.max(np.abs(z[..., 0]))
+    timeouts = ctypes.c_int(-1)
+    assert lib.tl_conv_status(ctypes.byref(timeouts)) == 0 and timeouts.value == 0
