@@ -319,6 +319,17 @@ __device__ __forceinline__ void tld16(uint32_t taddr, float (&v)[16]) {
   for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
 }
 
+// 8 consecutive FP32 accumulator columns of this thread's lane.
+__device__ __forceinline__ void tld8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = __uint_as_float(r[k]);
+}
+
 template <int CIN, int COUT>
 struct Smem {
   static constexpr int NC = CIN / 8;             // channel chunks of an input pixel
@@ -333,8 +344,10 @@ struct Smem {
 
 // Rows are pipelined: while the epilogue of row y reads its accumulators
 // from one tensor-memory buffer, the MMAs of row y + 1 run into the other.
+// Eight warps: warp w reads the lane quadrant w % 4 (pixels 32 (w % 4) ..
+// + 31) and the output-channel half w / 4 of the accumulators.
 template <int CIN, int COUT, int MODE>
-__global__ void __launch_bounds__(128) k_conv3x3_tc(ConvArgs a) {
+__global__ void __launch_bounds__(256) k_conv3x3_tc(ConvArgs a) {
   using S = Smem<CIN, COUT>;
   static_assert(COUT % 16 == 0 && COUT <= TCOLS && CIN % 16 == 0, "tile shape");
   constexpr uint32_t ID = idesc(128, COUT);
@@ -346,7 +359,8 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc(ConvArgs a) {
   uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 2);
   const int img = blockIdx.z, x0 = blockIdx.x * FTP, y0 = blockIdx.y * FRB;
   const int y1 = min(a.H, y0 + FRB);
-  const int tid = threadIdx.x, warp = tid >> 5;
+  constexpr int NT = 256, CH = COUT / 2;  // threads; output channels per thread
+  const int tid = threadIdx.x, warp = tid >> 5, quad = warp & 3, half = warp >> 2;
   const size_t plane = (size_t)a.H * a.W;
   const bf16 *xi = a.x + (size_t)img * plane * CIN;
 
@@ -361,13 +375,13 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc(ConvArgs a) {
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   if (tid < COUT) sbias[tid] = a.bias ? a.bias[tid] : 0.f;
-  for (int v = tid; v < COUT * S::KC; v += 128) {
+  for (int v = tid; v < COUT * S::KC; v += NT) {
     const int co = v / S::KC, kc = v % S::KC;
     cp_async16(sw + (kc * COUT + co) * 16, a.w + (size_t)co * 9 * CIN + kc * 8, 16);
   }
   auto load_row = [&](int yy) {
     unsigned char *dst = sx + ((yy + 4) & 3) * S::SLOT;
-    for (int v = tid; v < (FTP + 2) * S::NC; v += 128) {
+    for (int v = tid; v < (FTP + 2) * S::NC; v += NT) {
       const int col = v / S::NC, c8 = v % S::NC, xx = x0 + col - 1;
       const bool in = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
       const bf16 *src = in ? xi + ((size_t)yy * a.W + xx) * CIN + c8 * 8 : xi;
@@ -406,15 +420,16 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc(ConvArgs a) {
   const uint32_t tmem = *tslot;
   if (tid == 0) issue(y0, 0, tmem);
   uint32_t phases = 0u;  // bit b: the parity of mbarrier b's next completion
-  const int xx = x0 + tid;  // this thread's pixel in the epilogue
+  const int xx = x0 + 32 * quad + (tid & 31);  // this thread's pixel in the epilogue
   for (int y = y0; y < y1; ++y) {
     const int b = (y - y0) & 1;
     // MODE 2: the epilogue's GELU' inputs, loaded while the MMAs run
-    uint4 gzv[MODE == 2 ? COUT / 8 : 1];
+    uint4 gzv[MODE == 2 ? CH / 8 : 1];
     if (MODE == 2 && xx < a.W) {
-      const uint4 *gp = reinterpret_cast<const uint4 *>(a.gz + ((size_t)img * plane + (size_t)y * a.W + xx) * COUT);
+      const uint4 *gp =
+          reinterpret_cast<const uint4 *>(a.gz + ((size_t)img * plane + (size_t)y * a.W + xx) * COUT + half * CH);
 #pragma unroll
-      for (int q = 0; q < (MODE == 2 ? COUT / 8 : 1); ++q) gzv[q] = gp[q];
+      for (int q = 0; q < (MODE == 2 ? CH / 8 : 1); ++q) gzv[q] = gp[q];
     }
     bool done = false;
     for (int it = 0; it < SPIN_LIMIT && !done; ++it) done = bar_try(bar + b, (phases >> b) & 1u);
@@ -440,23 +455,30 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc(ConvArgs a) {
       if (tid == 0) issue(y + 1, b ^ 1, tmem);
     }
     fence_after();
-    float acc[COUT];
+    float acc[CH];
+    {
+      const uint32_t ta = tmem + ((uint32_t)(32 * quad) << 16) + b * TCOLS + half * CH;
+      if (CH == 16) {
+        float v[16];
+        tld16(ta, v);
 #pragma unroll
-    for (int c = 0; c < COUT; c += 16) {
-      float v[16];
-      tld16(tmem + ((uint32_t)(32 * warp) << 16) + b * TCOLS + c, v);
+        for (int k = 0; k < CH; ++k) acc[k] = v[k];
+      } else {
+        float v[8];
+        tld8(ta, v);
 #pragma unroll
-      for (int k = 0; k < 16; ++k) acc[c + k] = v[k];
+        for (int k = 0; k < CH; ++k) acc[k] = v[k];
+      }
     }
     fence_before();
     if (xx < a.W) {
       const size_t pix = (size_t)img * plane + (size_t)y * a.W + xx;
 #pragma unroll
-      for (int c = 0; c < COUT; ++c) acc[c] += sbias[c];
-      if (a.out32) a.out32[pix] = acc[0];
-      uint4 zo[COUT / 8], oo[COUT / 8];
+      for (int c = 0; c < CH; ++c) acc[c] += sbias[half * CH + c];
+      if (a.out32 && half == 0) a.out32[pix] = acc[0];
+      uint4 zo[CH / 8], oo[CH / 8];
 #pragma unroll
-      for (int q = 0; q < COUT / 8; ++q) {
+      for (int q = 0; q < CH / 8; ++q) {
         __nv_bfloat162 *zp = reinterpret_cast<__nv_bfloat162 *>(&zo[q]);
         __nv_bfloat162 *op = reinterpret_cast<__nv_bfloat162 *>(&oo[q]);
         const __nv_bfloat162 *gq = reinterpret_cast<const __nv_bfloat162 *>(&gzv[MODE == 2 ? q : 0]);
@@ -476,14 +498,14 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc(ConvArgs a) {
         }
       }
       if (MODE == 1 && a.z) {
-        uint4 *zd = reinterpret_cast<uint4 *>(a.z + pix * COUT);
+        uint4 *zd = reinterpret_cast<uint4 *>(a.z + pix * COUT + half * CH);
 #pragma unroll
-        for (int q = 0; q < COUT / 8; ++q) zd[q] = zo[q];
+        for (int q = 0; q < CH / 8; ++q) zd[q] = zo[q];
       }
       if (a.out) {
-        uint4 *od = reinterpret_cast<uint4 *>(a.out + pix * COUT);
+        uint4 *od = reinterpret_cast<uint4 *>(a.out + pix * COUT + half * CH);
 #pragma unroll
-        for (int q = 0; q < COUT / 8; ++q) od[q] = oo[q];
+        for (int q = 0; q < CH / 8; ++q) od[q] = oo[q];
       }
     }
   }
@@ -785,7 +807,7 @@ void launch_conv_mode(const ConvArgs &a, cudaStream_t st) {
     cudaFuncSetAttribute(tc::k_conv3x3_tc<CIN, COUT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     attr = true;
   }
-  tc::k_conv3x3_tc<CIN, COUT, MODE><<<grid, 128, smem, st>>>(a);
+  tc::k_conv3x3_tc<CIN, COUT, MODE><<<grid, 256, smem, st>>>(a);
 }
 
 template <int CIN, int COUT>
