@@ -437,7 +437,7 @@ def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     sub = ap.add_subparsers(dest="cmd", required=True)
     t = sub.add_parser("train")
-    t.add_argument("--out", default="gpurun_out/warmstart_net.bin")
+    t.add_argument("--out", default="warmstart_net.bin")
     t.add_argument("--decks512", type=int, default=192)
     t.add_argument("--decks2048", type=int, default=16)
     t.add_argument("--steps512", type=int, default=40)
