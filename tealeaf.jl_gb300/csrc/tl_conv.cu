@@ -239,8 +239,8 @@ __global__ void __launch_bounds__(128) k_conv3x3(ConvArgs a) {
 //               shifted by dx pixels: a descriptor, no im2col copy;
 //   weights:    [9 CIN/8 k chunks][COUT][8 k values]; core matrices 128 B apart
 //               along the output channels (SBO), k chunks COUT x 16 B apart (LBO).
-// Input rows live in a four-slot ring filled by cp.async (row y + 2 is
-// fetched while row y is computed).  The MMAs of a row complete on an
+// Input rows live in a ring of RING slots filled by cp.async, fetched
+// RING - 1 rows ahead of the row being computed.  The MMAs of a row complete on an
 // mbarrier (tcgen05.commit); every thread then reads its pixel's COUT
 // accumulators from its warp's tensor-memory lane quadrant (tcgen05.ld) for
 // the epilogue.  Every mbarrier wait is bounded: a wait that runs out stops
@@ -248,6 +248,17 @@ __global__ void __launch_bounds__(128) k_conv3x3(ConvArgs a) {
 namespace tc {
 
 __device__ int g_conv_timeouts;
+
+// cp.async.wait_group with a run-time count of groups allowed in flight (0..3).
+__device__ __forceinline__ void cp_async_wait_pending(int n) {
+  switch (n) {
+    case 0: asm volatile("cp.async.wait_group 0;\n" ::: "memory"); break;
+    case 1: asm volatile("cp.async.wait_group 1;\n" ::: "memory"); break;
+    case 2: asm volatile("cp.async.wait_group 2;\n" ::: "memory"); break;
+    default: asm volatile("cp.async.wait_group 3;\n" ::: "memory"); break;
+  }
+}
+constexpr int RING = 4;  // staged input rows: rows y - 1 .. y + 2 while row y is computed (six measured no faster)
 
 // GELU and its derivative with the hardware tanh (tanh.approx.f32, relative
 // error about 2^-11, below the BF16 rounding of the outputs).
@@ -337,7 +348,7 @@ struct Smem {
   static constexpr int SLOT = NC * ROWB;         // bytes of one staged input row
   static constexpr int KC = 9 * CIN / 8;         // k chunks of the weights
   static constexpr int WB = KC * COUT * 16;      // bytes of the weights
-  static constexpr int BIAS = WB + 4 * SLOT;     // COUT floats
+  static constexpr int BIAS = WB + RING * SLOT;  // COUT floats
   static constexpr int BAR = BIAS + 4 * COUT;    // two mbarriers and the tensor-memory address
   static constexpr int BYTES = BAR + 32;
 };
@@ -380,7 +391,7 @@ __global__ void __launch_bounds__(256) k_conv3x3_tc(ConvArgs a) {
     cp_async16(sw + (kc * COUT + co) * 16, a.w + (size_t)co * 9 * CIN + kc * 8, 16);
   }
   auto load_row = [&](int yy) {
-    unsigned char *dst = sx + ((yy + 4) & 3) * S::SLOT;
+    unsigned char *dst = sx + ((yy + RING) % RING) * S::SLOT;
     for (int v = tid; v < (FTP + 2) * S::NC; v += NT) {
       const int col = v / S::NC, c8 = v % S::NC, xx = x0 + col - 1;
       const bool in = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
@@ -394,7 +405,7 @@ __global__ void __launch_bounds__(256) k_conv3x3_tc(ConvArgs a) {
     const uint32_t d = tmem + b * TCOLS;
 #pragma unroll
     for (int dy = 0; dy < 3; ++dy) {
-      const uint32_t rbase = xbase + ((y - 1 + dy + 4) & 3) * S::SLOT;
+      const uint32_t rbase = xbase + ((y - 1 + dy + RING) % RING) * S::SLOT;
 #pragma unroll
       for (int dx = 0; dx < 3; ++dx) {
         const int tap = 3 * dy + dx;
@@ -408,11 +419,18 @@ __global__ void __launch_bounds__(256) k_conv3x3_tc(ConvArgs a) {
     }
     commit(bar + b);
   };
-  // rows y0 - 1 .. y0 + 2 (row y0 + 2 feeds the MMAs of row y0 + 1)
-  for (int r = -1; r <= 2; ++r)
+  // rows y0 - 1 .. y0 + 1 for the first MMAs, then y0 + 2 .. y0 + RING - 2,
+  // one group each, in flight
+  for (int r = -1; r <= 1; ++r)
     if (y0 + r <= y1) load_row(y0 + r);
   cp_async_commit();
-  cp_async_wait_all();
+  for (int r = 2; r <= RING - 2; ++r)
+    if (y0 + r <= y1) {
+      load_row(y0 + r);
+      cp_async_commit();
+    }
+  // the first group (weights, rows y0 - 1 .. y0 + 1) must have landed
+  cp_async_wait_pending(min(max(y1 - (y0 + 1), 0), RING - 3));
   fence_async_smem();
   fence_before();
   __syncthreads();
@@ -438,16 +456,15 @@ __global__ void __launch_bounds__(256) k_conv3x3_tc(ConvArgs a) {
       if (tid == 0) atomicAdd(&g_conv_timeouts, 1);
       break;
     }
-    // the MMAs of row y are done: row y - 1's slot takes row y + 3
-    const bool more = y + 3 <= y1;
-    if (more) {
-      load_row(y + 3);
+    // the MMAs of row y are done: row y - 1's slot takes row y + RING - 1
+    if (y + RING - 1 <= y1) {
+      load_row(y + RING - 1);
       cp_async_commit();
     }
     if (y + 1 < y1) {
-      // row y + 2 (the group before the newest) must have landed
-      if (more) asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-      else cp_async_wait_all();
+      // row y + 2 must have landed; the rows after it, up to y + RING - 1, may
+      // still be in flight (one group per row)
+      cp_async_wait_pending(min(max(y1 - (y + 2), 0), RING - 3));
       fence_async_smem();
       fence_before();
       __syncthreads();
