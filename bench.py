@@ -243,7 +243,7 @@ KERNELS = {"fp64": ((0, "cg_w_step", W_STEP_BYTES), (1, "cg_ur_step", UR_STEP_BY
 # DRAM bytes (read + write) per interior cell of one launch, from the ncu
 # captures at 4096^2 summarised in profiles/*_4096.md; traffic grows with the
 # cells, so a full launch moves this times n^2.
-TRAFFIC_BYTES_PER_CELL = {"ir_dir_step": 247.5e6 / 4096 ** 2, "ir_update_step": 361.1e6 / 4096 ** 2,
+TRAFFIC_BYTES_PER_CELL = {"ir_dir_step": 247.4e6 / 4096 ** 2, "ir_update_step": 362.5e6 / 4096 ** 2,
                           "cg_w_step": 923.7e6 / 4096 ** 2}
 
 
