@@ -104,8 +104,9 @@ __device__ __forceinline__ void ir_cg_epilogue(const Fields &F, double rrn, cuda
 // OpIrDir forms p' = beta p + r and p'.A p' and stores p' (reads p, r, iw:
 // 16 B per cell with the store); OpIrUpdate recomputes w = A p' from the
 // stored p' and does x += alpha p', r -= alpha w, r.r (reads p', iw, x, r,
-// writes x, r: 24 B).  Against OpIrW + OpIrUR (48 B) neither w nor Kx, Ky is
-// stored: the faces come from the inverse weights, Kx = rx/2 (iw_l + iw_c).
+// writes x, r: 24 B).  Neither w nor Kx, Ky is stored (a pair that stored
+// them would move 48 B): the faces come from the inverse weights,
+// Kx = rx/2 (iw_l + iw_c).
 // Both kernels evaluate the stencil with the same function on the same
 // floats, so the w of the update equals the w of the dot bit for bit.
 
