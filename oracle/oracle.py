@@ -47,7 +47,7 @@ class Settings(C.Structure):
 
 class Opts(C.Structure):
     _fields_ = [("mode", C.c_int), ("order", C.c_int), ("dev_warps", C.c_int), ("dev_rows", C.c_int),
-                ("dev_blocks", C.c_int), ("nthreads", C.c_int)]
+                ("dev_blocks", C.c_int), ("nthreads", C.c_int), ("criterion", C.c_int)]
 
 
 class Chunk(C.Structure):
@@ -61,7 +61,8 @@ class Chunk(C.Structure):
 
 class Result(C.Structure):
     _fields_ = [("iters", C.c_int), ("cg_iters", C.c_int), ("inner_iters", C.c_int), ("est_iters", C.c_int),
-                ("error", C.c_double), ("eigmin", C.c_double), ("eigmax", C.c_double), ("status", C.c_int)]
+                ("error", C.c_double), ("eigmin", C.c_double), ("eigmax", C.c_double), ("status", C.c_int),
+                ("converged", C.c_int), ("rel_residual", C.c_double)]
 
 
 class Summary(C.Structure):
@@ -140,9 +141,11 @@ def parse_deck(text: str) -> Settings:
     return s
 
 
-def make_opts(mode=MODE_TEALEAF, order=ORDER_REFERENCE, layout=None, nthreads=1) -> Opts:
+def make_opts(mode=MODE_TEALEAF, order=ORDER_REFERENCE, layout=None, nthreads=1, criterion=0) -> Opts:
+    """criterion 1: CG's relative test on the recursive then the true residual
+    (the GPU library's TL_CRIT_RELATIVE); 0: the reference's own test."""
     o = Opts()
-    o.mode, o.order, o.nthreads = mode, order, nthreads
+    o.mode, o.order, o.nthreads, o.criterion = mode, order, nthreads, criterion
     if layout is not None:
         o.dev_warps, o.dev_rows, o.dev_blocks = layout
     return o

@@ -93,26 +93,30 @@ double tlo_device_sum(const double *v, int nx, int ny, const tlo_opts *o) {
   double *partial = (double *)calloc((size_t)G, sizeof(double));
   double *acc = (double *)malloc(sizeof(double) * (size_t)F);
   if (!partial || !acc) { free(partial); free(acc); return NAN; }
+  /* Blocks are independent until the last block's pass, so they may be
+   * computed by several host threads without changing any partial. */
+#pragma omp parallel for num_threads(NT(o)) schedule(dynamic, 1)
   for (int b = 0; b < G; ++b) {
-    for (int t = 0; t < F; ++t) acc[t] = 0.0;
+    double bacc[32 * 32];
+    for (int t = 0; t < F; ++t) bacc[t] = 0.0;
     for (long long t = b; t < T; t += G) {
       const long long tx = t % ntx, ty = t / ntx;
       const int j0 = (int)(ty * TY), j1 = (int)((ty * TY + TY) < ny ? ty * TY + TY : ny);
       for (int w = 0; w < NW; ++w)
         for (int l = 0; l < 32; ++l) {
           const long long i0 = tx * TW + 64 * w + 2 * l;
-          double a = acc[w * 32 + l];
+          double a = bacc[w * 32 + l];
           for (int j = j0; j < j1; ++j) {
             if (i0 < nx) a += v[i0 + (size_t)j * nx];
             if (i0 + 1 < nx) a += v[i0 + 1 + (size_t)j * nx];
           }
-          acc[w * 32 + l] = a;
+          bacc[w * 32 + l] = a;
         }
     }
     double blk = 0.0;
     for (int w = 0; w < NW; ++w) {
-      warp_butterfly(acc + 32 * w);
-      blk = (w == 0) ? acc[0] : blk + acc[32 * w];
+      warp_butterfly(bacc + 32 * w);
+      blk = (w == 0) ? bacc[0] : blk + bacc[32 * w];
     }
     partial[b] = blk;
   }
@@ -783,7 +787,45 @@ static double cg_mainstep(tlo_chunk *c, int tt, double rro, const tlo_opts *o) {
   return rrn;
 }
 
-/* solve! (CG.jl:7-29) */
+/* a.a over the interior (the relative criterion's bb = u0.u0), summed in the
+ * order the options select. */
+static double interior_dot(tlo_chunk *c, const double *a, const tlo_opts *o) {
+  const int X = c->x, Y = c->y, hd = c->hd, nx = X - 2 * hd;
+  double acc = 0.0;
+  const int store = o->order != TLO_ORDER_THREADS;
+#pragma omp parallel for num_threads(NT(o)) schedule(static) reduction(+ : acc)
+  for (int j = hd; j < Y - hd; ++j)
+    for (int i = hd; i < X - hd; ++i) {
+      const double v = a[IDX(i, j)] * a[IDX(i, j)];
+      if (store) g_scr.interior[(size_t)(i - hd) + (size_t)(j - hd) * nx] = v; else acc += v;
+    }
+  return store ? reduce_interior(c, o, SEQ) : acc;
+}
+
+/* The true residual t = u0 - A u over the interior; returns t.t.  With
+ * `write`, r = p = t (the restart of the relative criterion). */
+static double true_residual(tlo_chunk *c, const tlo_opts *o, int write) {
+  const int X = c->x, Y = c->y, hd = c->hd, nx = X - 2 * hd;
+  double *u = c->f[TLO_U], *u0 = c->f[TLO_U0], *r = c->f[TLO_R], *p = c->f[TLO_P];
+  double acc = 0.0;
+  const int store = o->order != TLO_ORDER_THREADS;
+#pragma omp parallel for num_threads(NT(o)) schedule(static) reduction(+ : acc)
+  for (int j = hd; j < Y - hd; ++j)
+    for (int i = hd; i < X - hd; ++i) {
+      const size_t id = IDX(i, j);
+      const double t = u0[id] - smvp(c, u, i, j, o->mode);
+      if (write) r[id] = p[id] = t;
+      const double v = t * t;
+      if (store) g_scr.interior[(size_t)(i - hd) + (size_t)(j - hd) * nx] = v; else acc += v;
+    }
+  return store ? reduce_interior(c, o, SEQ) : acc;
+}
+
+/* solve! (CG.jl:7-29).  With o->criterion == 1 (not in the reference, which
+ * tests sqrt|rr| < eps, CG.jl:24) the loop tests sqrt(|rr| / bb) < eps with
+ * bb = u0.u0, including before the first iteration; once it holds, the true
+ * residual u0 - A u is measured, and while its relative norm is above eps
+ * (and iterations remain) CG restarts from it: r = p = u0 - A u. */
 static int cg_solve(tlo_chunk *c, tlo_settings *s, const tlo_opts *o, double rx, double ry, tlo_result *res) {
   double rro;
   int rc = tlo_cg_init(c, s->coefficient, rx, ry, o, &rro);
@@ -791,17 +833,44 @@ static int cg_solve(tlo_chunk *c, tlo_settings *s, const tlo_opts *o, double rx,
   const int up[2] = {TLO_EX_U, TLO_EX_P};
   if ((rc = tlo_halo_update(c, s, o, 1, up, 2, 1))) return rc;
   tlo_copy_u(c, o);
+  const int rel = o->criterion == 1;
+  const double bb = rel ? interior_dot(c, c->f[TLO_U0], o) : 0.0;
   double error = ERROR_START;
   int iters = 0;
-  for (int tt = 1; tt <= s->maxiters; ++tt) {
-    iters = tt;
-    rro = error = cg_mainstep(c, tt, rro, o);
-    if ((rc = tlo_halo_update(c, s, o, 1, NULL, -1, 1))) return rc;
-    if (sqrt(fabs(error)) < s->eps) break;
+  res->rel_residual = -1.0;
+  if (rel) {
+    const double rel0 = bb > 0 ? sqrt(rro / bb) : sqrt(rro);
+    if (rel0 < s->eps) {
+      res->iters = res->cg_iters = 0;
+      res->error = rro;
+      res->converged = 1;
+      res->rel_residual = rel0;
+      return TLO_OK;
+    }
+  }
+  int converged = 0;
+  for (int restart = 0; restart < 8; ++restart) {
+    for (int tt = iters + 1; tt <= s->maxiters; ++tt) {
+      iters = tt;
+      rro = error = cg_mainstep(c, tt, rro, o);
+      if ((rc = tlo_halo_update(c, s, o, 1, NULL, -1, 1))) return rc;
+      if (rel ? sqrt(fabs(error) / bb) < s->eps : sqrt(fabs(error)) < s->eps) {
+        converged = 1;
+        break;
+      }
+    }
+    if (!rel) break;
+    const double tr = true_residual(c, o, 0);
+    res->rel_residual = bb > 0 ? sqrt(tr / bb) : sqrt(tr);
+    converged = res->rel_residual < s->eps;
+    if (converged || o->mode == TLO_MODE_REFERENCE || iters >= s->maxiters) break;
+    rro = true_residual(c, o, 1);
+    if ((rc = tlo_halo_update(c, s, o, 1, up, 2, 1))) return rc;
   }
   res->iters = iters;
   res->cg_iters = iters;
   res->error = error;
+  res->converged = converged;
   return TLO_OK;
 }
 
@@ -1219,6 +1288,7 @@ static int jacobi_solve(tlo_chunk *c, tlo_settings *s, const tlo_opts *o, double
 
 int tlo_solve(tlo_chunk *c, tlo_settings *s, const tlo_opts *o, double rx, double ry, tlo_result *res) {
   memset(res, 0, sizeof *res);
+  res->rel_residual = -1.0;
   if (!ensure_scratch(c)) return TLO_ERR_NOMEM;
   int rc;
   switch (s->solver) {

@@ -108,6 +108,9 @@ typedef struct {
   int dev_rows;     /* rows of cells one warp walks per tile   */
   int dev_blocks;   /* persistent blocks in the grid           */
   int nthreads;     /* OpenMP threads for elementwise loops (1 = scalar) */
+  int criterion;    /* CG only: 0 the reference's sqrt|rr| < eps (CG.jl:24); 1 the relative test
+                       sqrt(|rr| / u0.u0) < eps on the recursive residual, then on the true residual
+                       u0 - A u, restarting from it (at most 8 times) while it is above eps */
 } tlo_opts;
 
 typedef struct {
@@ -126,6 +129,8 @@ typedef struct {
   double error;     /* the error value the solver loop ended with      */
   double eigmin, eigmax;
   int status;       /* TLO_OK or an error code                          */
+  int converged;    /* CG: the loop ended on its convergence test       */
+  double rel_residual; /* CG with criterion 1: ||u0 - A u|| / ||u0|| at the end, else -1 */
 } tlo_result;
 
 typedef struct {

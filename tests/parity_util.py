@@ -81,11 +81,11 @@ def gpu_run(tl, text: str, mode: int, exact: bool = False, steps_fields: bool = 
 
 
 def oracle_run(text: str, mode: int, order: int = O.ORDER_REFERENCE, layout=None, steps_fields=False,
-               solver: str | None = None):
+               solver: str | None = None, criterion: int = 0, nthreads: int = 1):
     s = O.parse_deck(text)
     if solver:
         s.solver = SOLVER_CODES[solver]
-    o = O.make_opts(mode=mode, order=order, layout=layout)
+    o = O.make_opts(mode=mode, order=order, layout=layout, criterion=criterion, nthreads=nthreads)
     ch = O.OracleChunk(s, o)
     ch.initialise()
     if not steps_fields:

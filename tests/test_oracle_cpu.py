@@ -207,3 +207,76 @@ def test_golden(case):
     assert got["steps"] == case["steps"]
     assert got["summaries"] == case["summaries"]
     assert got["u_checksum"] == case["u_checksum"]
+
+
+# ---------------------------------------------------------------------------
+# the relative criterion against a direct sparse solve
+# ---------------------------------------------------------------------------
+
+def _operator_from_fields(kx, ky, hd):
+    """The tealeaf-mode 5-point operator of the oracle's Kx, Ky (interior
+    cells, reflective boundary: a neighbour across the edge is the cell
+    itself, so that coupling drops out) as a scipy sparse matrix."""
+    import scipy.sparse as sp
+    X, Y = kx.shape
+    nx, ny = X - 2 * hd, Y - 2 * hd
+    idx = np.arange(nx * ny).reshape(ny, nx).T          # idx[i, j], i fastest
+    rows, cols, vals = [], [], []
+    diag = np.ones((nx, ny))
+    for di, dj, k in ((1, 0, kx[hd + 1:X - hd + 1, hd:Y - hd]), (-1, 0, kx[hd:X - hd, hd:Y - hd]),
+                      (0, 1, ky[hd:X - hd, hd + 1:Y - hd + 1]), (0, -1, ky[hd:X - hd, hd:Y - hd])):
+        ii, jj = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+        ni, nj = ii + di, jj + dj
+        inside = (ni >= 0) & (ni < nx) & (nj >= 0) & (nj < ny)
+        diag += np.where(inside, k, 0.0)
+        rows.append(idx[inside])
+        cols.append(idx[ni[inside], nj[inside]])
+        vals.append(-k[inside])
+    rows.append(idx.ravel())
+    cols.append(idx.ravel())
+    vals.append(diag.ravel())
+    n = nx * ny
+    return sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(n, n))
+
+
+@pytest.mark.parametrize("nx,ny,seed", [(40, 40, 3), (57, 31, 4)])
+def test_relative_criterion_against_direct_solve(nx, ny, seed):
+    """CG with the relative criterion (the GPU library's TL_CRIT_RELATIVE)
+    stops with ||u0 - A u|| / ||u0|| < eps, checked on the true residual, and
+    its u equals scipy's direct sparse solve of the same 5-point system
+    to the accuracy that residual allows."""
+    import scipy.sparse.linalg as spla
+    text = random_deck(nx, seed, ny=ny, steps=1, eps=1e-10)
+    s = O.parse_deck(text)
+    ch = O.OracleChunk(s, O.make_opts(mode=O.MODE_TEALEAF, criterion=1))
+    ch.initialise()
+    ch.halo(1, ["energy", "density"])
+    r = ch.solve(s.dtinit / s.dx ** 2, s.dtinit / s.dy ** 2)
+    assert r.converged and 0 <= r.rel_residual < 1e-10
+    hd = s.halodepth
+    A = _operator_from_fields(ch.field("kx"), ch.field("ky"), hd)
+    u0 = ch.field("u0")[hd:-hd, hd:-hd]
+    u = ch.field("u")[hd:-hd, hd:-hd]
+    exact = spla.spsolve(A.tocsc(), u0.T.ravel()).reshape(ny, nx).T
+    true_rel = np.linalg.norm(u0.T.ravel() - A @ u.T.ravel()) / np.linalg.norm(u0)
+    assert abs(true_rel - r.rel_residual) <= 1e-3 * r.rel_residual + 1e-16
+    assert np.max(np.abs(u - exact)) <= 1e-8 * np.max(np.abs(exact))
+
+
+def test_relative_criterion_edges():
+    """Near the rounding floor (eps 1e-14) the loop ends converged on the true
+    residual or out of restarts with it measured; a tolerance the start
+    already meets stops before the first iteration (no 0/0 alpha)."""
+    text = random_deck(48, 9, steps=1, eps=1e-14)
+    s = O.parse_deck(text)
+    ch = O.OracleChunk(s, O.make_opts(mode=O.MODE_TEALEAF, criterion=1))
+    ch.initialise()
+    ch.halo(1, ["energy", "density"])
+    r = ch.solve(s.dtinit / s.dx ** 2, s.dtinit / s.dy ** 2)
+    assert r.rel_residual >= 0 and (bool(r.converged) == (r.rel_residual < 1e-14))
+    s2 = O.parse_deck(random_deck(48, 9, steps=1, eps=10.0))
+    ch2 = O.OracleChunk(s2, O.make_opts(mode=O.MODE_TEALEAF, criterion=1))
+    ch2.initialise()
+    ch2.halo(1, ["energy", "density"])
+    r2 = ch2.solve(s2.dtinit / s2.dx ** 2, s2.dtinit / s2.dy ** 2)
+    assert r2.converged and r2.iters == 0 and 0 <= r2.rel_residual < 10.0
