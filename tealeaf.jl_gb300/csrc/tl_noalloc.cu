@@ -6,8 +6,17 @@
 // __device__ array, not memory obtained from cudaMalloc: every GPU that loads
 // this library holds one copy (about 33 KB) until the process exits, and every
 // call on that GPU shares it.
+//
+// Host code cannot use the array's name as a device address, so the address
+// is looked up with cudaGetSymbolAddress, with the device current, the first
+// time a call runs in a device context.  The lookup is keyed on the context's
+// id: after cudaDeviceReset the primary context is created again, the module
+// is loaded again and the array may move, so a call in the new context looks
+// the address up again instead of writing through a stale one.
 #include <cstdio>
 #include <mutex>
+
+#include <cuda.h>
 
 #include "tl_walk.cuh"
 
@@ -16,13 +25,46 @@ namespace {
 constexpr int NOALLOC_MAX_BLOCKS = 1024;                                 // block partials the scratch holds
 constexpr int NOALLOC_SCRATCH = tl::MAX_RED * NOALLOC_MAX_BLOCKS + 32;  // + the ticket, in doubles
 constexpr long long NOALLOC_MAX_CELLS = 2147483647LL;                    // interior cells per call
+// Per-dimension limits: the tile walk forms column and row indices, tile
+// counts and hd + i in int, so xcells + 2*halodepth plus one tile width (256
+// columns) and ycells + 2*halodepth plus one tile height (8 rows) must stay
+// below INT_MAX.  These bounds keep every such sum far from it.
+constexpr int NOALLOC_MAX_DIM = 1 << 30;                                 // xcells, ycells
+constexpr int NOALLOC_MAX_HALO = 1 << 20;                                // halodepth
 constexpr int MAX_DEVICES = 64;
 
 static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_SCRATCH];
 
 std::mutex g_setup_mutex;
 double *g_scratch_addr[MAX_DEVICES];
+unsigned long long g_scratch_ctx[MAX_DEVICES];  // id of the context the address was looked up in
 int g_sm_count[MAX_DEVICES];
+
+// cuCtxGetCurrent and cuCtxGetId through the runtime's driver entry points
+// (the library links the static runtime, not libcuda).
+typedef CUresult (*PFN_ctxGetCurrent)(CUcontext *);
+typedef CUresult (*PFN_ctxGetId)(CUcontext, unsigned long long *);
+PFN_ctxGetCurrent g_ctx_get_current;
+PFN_ctxGetId g_ctx_get_id;
+
+// Id of the current context, 0 when there is none; the caller holds the mutex.
+unsigned long long current_context_id() {
+  if (!g_ctx_get_current || !g_ctx_get_id) {
+    cudaDriverEntryPointQueryResult q1, q2;
+    void *f1 = nullptr, *f2 = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess || !f1 ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+        q2 != cudaDriverEntryPointSuccess || !f2)
+      return 0;
+    g_ctx_get_current = reinterpret_cast<PFN_ctxGetCurrent>(f1);
+    g_ctx_get_id = reinterpret_cast<PFN_ctxGetId>(f2);
+  }
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (g_ctx_get_current(&c) != CUDA_SUCCESS || !c || g_ctx_get_id(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 // vol, mass = vol*rho, ie = mass*energy, temp = mass*u over the interior, in
 // the same order and reduction tree as the context's field summary.
@@ -65,6 +107,10 @@ extern "C" int tl_field_summary_noalloc(const double *volume, const double *dens
     return fail(err, errlen, TL_ERR_ARG, "tl_field_summary_noalloc: null array pointer");
   if (xcells < 1 || ycells < 1 || halodepth < 1)
     return fail(err, errlen, TL_ERR_ARG, "tl_field_summary_noalloc: cells and halo depth must be >= 1");
+  if (xcells > NOALLOC_MAX_DIM || ycells > NOALLOC_MAX_DIM || halodepth > NOALLOC_MAX_HALO)
+    return fail(err, errlen, TL_ERR_ARG,
+                "tl_field_summary_noalloc: xcells, ycells above the maximum of 1073741824 per dimension or "
+                "halodepth above 1048576");
   if ((long long)xcells * ycells > NOALLOC_MAX_CELLS)
     return fail(err, errlen, TL_ERR_ARG,
                 "tl_field_summary_noalloc: xcells*ycells exceeds the maximum of 2147483647 interior cells");
@@ -77,11 +123,14 @@ extern "C" int tl_field_summary_noalloc(const double *volume, const double *dens
   double *scratch = nullptr;
   int sms = 0;
   {
-    // First call on this device: look up the device address of the scratch
-    // array with this device current.  Host code cannot use the array's
-    // name as an address.
+    // First call in this device's current context: look up the device
+    // address of the scratch array with this device current.  Host code
+    // cannot use the array's name as an address.  A context created again
+    // (after cudaDeviceReset) has a new id and gets a new lookup.
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_addr[dev]) {
+    const unsigned long long ctx = current_context_id();
+    if (!ctx) return fail(err, errlen, TL_ERR_CUDA, "tl_field_summary_noalloc: no current device context");
+    if (!g_scratch_addr[dev] || g_scratch_ctx[dev] != ctx) {
       void *p = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
       if (e != cudaSuccess) {
@@ -94,6 +143,7 @@ extern "C" int tl_field_summary_noalloc(const double *volume, const double *dens
       if (e != cudaSuccess || n < 1) return fail(err, errlen, TL_ERR_CUDA, "tl_field_summary_noalloc: no SM count");
       g_sm_count[dev] = n;
       g_scratch_addr[dev] = static_cast<double *>(p);
+      g_scratch_ctx[dev] = ctx;
     }
     scratch = g_scratch_addr[dev];
     sms = g_sm_count[dev];
