@@ -95,11 +95,13 @@ typedef struct {
   int precision;            /* TL_PREC_*                                     */
   int exact;                /* 1: tealeaf mode reproduces the reference's operation order with no FMA
                                contraction (bit-identical to the CPU restatement); 0: fused FMA kernels */
-  int warmstart;            /* CG in tealeaf mode: 0 off; TL_WARM_NETWORK: start from the warm-start
-                               network's prediction when it beats the plain start (tl_warm_load);
-                               TL_WARM_EXTRAPOLATE: the same with u^n + (u^n - u^{n-1}), no network */
+  int warmstart;            /* CG in tealeaf mode, the start when it beats the plain start u^n by
+                               residual: 0 off; TL_WARM_NETWORK: the A-norm projection onto u^n, the
+                               last three increments and the warm-start network's correction
+                               (tl_warm_load); TL_WARM_HISTORY: the same projection without the
+                               network; TL_WARM_EXTRAPOLATE: u^n + (u^n - u^{n-1}) */
 } tl_params;
-enum { TL_WARM_OFF = 0, TL_WARM_NETWORK = 1, TL_WARM_EXTRAPOLATE = 2 };
+enum { TL_WARM_OFF = 0, TL_WARM_NETWORK = 1, TL_WARM_EXTRAPOLATE = 2, TL_WARM_HISTORY = 3 };
 
 typedef struct {
   int iters;                /* trips of the solver's main loop                  */
@@ -114,10 +116,12 @@ typedef struct {
   int launches;             /* kernels this solve launched (graph-body kernels counted per trip) */
   int warm;                 /* 0: plain start (no warm start asked or no previous step), 1: the
                                prediction was used, 2: the prediction lost to the plain start,
-                               3: no prediction (paused after predictions that cost iterations),
-                               4: no prediction (a control solve from the plain start) */
+                               3 (TL_WARM_NETWORK): the projection without the network's term had
+                               the smaller residual and was used */
   double r0_plain;          /* ||u0 - A u^n|| / ||u0|| of the plain start (warm start asked), else -1 */
   double r0_pred;           /* the same for the prediction, -1 when none was made */
+  double warm_coef[5];      /* the prediction's weights on u^n, u^{n-1}, u^{n-2}, u^{n-3} and on the
+                               network's correction g (u^n - u^{n-1}); zero when no prediction */
 } tl_result;
 
 /* Creation.  Replaces Chunk(set) (src/chunk.jl:68-89): allocates every field
@@ -198,8 +202,9 @@ int tl_timer_stop(tl_ctx *ctx, double *ms);
  * Chebyshev step, 5: a PPCG inner sweep, 6: the FP32 Chebyshev step, 7: an
  * FP32 PPCG inner sweep, 8: the FP32 CG direction step p' = beta p + r with
  * p'.A p', 9: the FP32 CG update step with A p' recomputed; 8 and 9 are the
- * FP32 CG iteration; 2 and 3, an earlier FP32 pair, are retired and return
- * TL_ERR_ARG) on the current fields; for roofline measurements.  The launches overwrite
+ * FP32 CG iteration; 10: a Jacobi sweep, 11: the depth-1 halo update of u and
+ * p, 12: PPCG's outer u/r update; 2 and 3, an earlier FP32 pair, are retired
+ * and return TL_ERR_ARG) on the current fields; for roofline measurements.  The launches overwrite
  * solver work fields (p, w, r, u, sd, their second buffers and the FP32
  * copies): call it after the solves whose fields matter. */
 int tl_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch);
@@ -229,13 +234,15 @@ int tl_batch_last_ms(tl_batch *batch, double *ms);  /* device time of the last b
  * (X, Y) arrays, X = xcells + 2*halodepth, `pitch` doubles between columns;
  * out: device pointer to 4 doubles; stream: a cudaStream_t (NULL = legacy
  * default stream); err/errlen: optional buffer for the error message.
- * Limits: at most 2147483647 interior cells per call; larger sizes are
+ * Limits: at most 2147483647 interior cells per call, xcells and ycells at
+ * most 1073741824 each and halodepth at most 1048576; larger sizes are
  * rejected with TL_ERR_ARG.
  * The reduction scratch (4 x 1024 block partials and a ticket, about 33 KB)
  * is a static device array: each GPU that loads the library holds it until
- * the process exits.  The first call on each device looks up its address
- * (cudaGetSymbolAddress) with that device current, so make that first call
- * before any stream capture.  All calls on a device share the scratch: calls
+ * the process exits.  The first call in each device context looks up its
+ * address (cudaGetSymbolAddress) with that device current, so make that first
+ * call before any stream capture; after cudaDeviceReset the next call is a
+ * first call again.  All calls on a device share the scratch: calls
  * that overlap on the GPU (different streams, no ordering) race and give
  * wrong sums.  The call is asynchronous on `stream`. */
 int tl_field_summary_noalloc(const double *volume, const double *density, const double *energy, const double *u,
@@ -266,14 +273,18 @@ int tl_parse_deck(const char *text, int mode, tl_deck *deck, tl_state *states, i
  * No counterpart in the reference.  A 6-layer 3x3 convolutional network (32
  * channels, GELU between layers, BF16 weights, FP32 accumulation on the
  * tensor cores) reads, per cell, u^n / rms(u^n), log(rx / density) / 4 and
- * (u^n - u^{n-1}) / rms(u^n - u^{n-1}) and returns a factor g; the predicted
- * solution is u^n + (1 + g) (u^n - u^{n-1}).  CG starts from it only when its
- * residual ||u^n - A x|| is below the plain start's; it must still meet eps on
- * the true residual.  A smaller initial residual does not imply fewer
- * iterations, so runs of at most `trust` (2, 4, ... 32) solves from the
- * prediction are bracketed by control solves from the plain start; a run that
- * needed more iterations than its controls, or a network prediction the
- * residual test rejected, pauses the prediction for 4, 8, ... 64 steps.
+ * (u^n - u^{n-1}) / rms(u^n - u^{n-1}) and returns a factor g; its prediction
+ * of u^{n+1} is u^n + (1 + g) (u^n - u^{n-1}).  In the solve, the start is
+ * the A-norm projection of the solution onto u^n, the last three increments
+ * u^{n-k} - u^{n-k-1} and the network's correction g (u^n - u^{n-1}): the
+ * combination closest to A^{-1} u^n in the A-norm, so never farther than the
+ * plain start or the linear extrapolation.  The network's term is kept only
+ * when that candidate's residual ||u^n - A x|| is below the residual of the
+ * same projection without it; after a step where it was not, the next 1, 2,
+ * 4, ... 32 steps (doubling with each such step, back to 1 after a step where
+ * it was) skip the network.  CG starts from the prediction only when its
+ * residual is below the plain start's, and must still meet eps on the true
+ * residual.
  *
  * Parameter vector (FP32, TL_WARM_NPARAMS values), layer by layer:
  * W[cout][9][cin] then b[cout], with (cin, cout) = (16, 32), (32, 32) x 4,

@@ -56,6 +56,7 @@ class SolveResult:
     warm: int = 0              # 0 plain start, 1 the prediction was used, 2 it lost to the plain start
     r0_plain: float = -1.0     # initial relative residual of the plain start (warm start asked)
     r0_pred: float = -1.0      # the same for the prediction (-1: none made)
+    warm_coef: tuple = ()      # the prediction's weights on u^n, u^{n-1}, u^{n-2}, u^{n-3}, network term
 
 
 class Chunk:
@@ -247,7 +248,7 @@ def _solve(chunk: Chunk, settings: Settings, rx: float, ry: float, solver: int) 
         settings.toexchange["u"] = True
     r = SolveResult(res.iters, res.cg_iters, res.inner_iters, res.est_iters, res.error, res.eigmin, res.eigmax,
                     bool(res.converged), res.refinements, res.rel_residual, ms.value, res.launches, res.warm,
-                    res.r0_plain, res.r0_pred)
+                    res.r0_plain, res.r0_pred, tuple(res.warm_coef))
     log.info("solve complete iters=%d error=%r", r.iters, r.error)
     return r
 

@@ -422,8 +422,9 @@ extern "C" int tl_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per
     tl_set_error(ctx, "kernel %d: the 48-byte FP32 pair is retired (8 and 9 are the FP32 CG iteration)", kernel);
     return TL_ERR_ARG;
   }
-  if (kernel < 0 || kernel > 5) return TL_ERR_ARG;
-  launch_init_diag(ctx->stream, F, ctx->g);
+  if (kernel < 0 || kernel > 12) return TL_ERR_ARG;
+  if (kernel == 10) launch_init_rdiag(ctx->stream, F, ctx->g);  // the fused Jacobi sweep's reciprocal diagonal
+  else launch_init_diag(ctx->stream, F, ctx->g);
   CKL();
   CK(cudaEventRecord(ctx->tev0, ctx->stream));
   for (int k = 0; k < reps; ++k) {
@@ -432,9 +433,20 @@ extern "C" int tl_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per
     else if (kernel == 4)
       launch_cheby_step(ctx->stream, F, ctx->g, ctx->walk_w64, (k & 1) ? F.ub : F.u, (k & 1) ? F.u : F.ub, 0, 0, 0, 0,
                         0);
-    else
+    else if (kernel == 5)
       launch_ppcg_inner(ctx->stream, F, ctx->g, ctx->walk_w64, (k & 1) ? F.sdb : F.sd, (k & 1) ? F.sd : F.sdb, 1, 0, 0,
                         0, 0, 0);
+    else if (kernel == 10)  // the fused Jacobi sweep, on the layout the fused Jacobi solve uses
+      launch_jacobi(ctx->stream, F, ctx->g, ctx->walk_w64, (k & 1) ? F.ub : F.u, (k & 1) ? F.u : F.ub, 0, 0);
+    else if (kernel == 11) {  // haloupdate! of u and p at depth 1 (CG.jl:23)
+      double *ptrs[2] = {F.u, F.p};
+      launch_halo(ctx->stream, ptrs, 2, ctx->g, 1, TL_MODE_TEALEAF);
+    } else if (kernel == 12)  // PPCG's outer u/r update with sd = r / theta
+      launch_ppcg_ur(ctx->stream, F, ctx->g, ctx->walk_ur64, F.p, F.sd, 0, 0);
+    else {
+      tl_set_error(ctx, "kernel %d has no benchmark", kernel);
+      return TL_ERR_ARG;
+    }
   }
   CKL();
   CK(cudaEventRecord(ctx->tev1, ctx->stream));

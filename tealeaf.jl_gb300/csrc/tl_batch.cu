@@ -17,7 +17,9 @@
 // residual, test) for the decks whose inner loop just ended; the test either
 // finishes the deck or restarts its inner loop from the true residual, all on
 // the device.
+#include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -447,6 +449,49 @@ int bfail(tl_batch *b, cudaError_t e, const char *what) {
     if (e_ != cudaSuccess) return bfail(b, e_, #x); \
   } while (0)
 
+// One trip of the batched loop: two CG iterations of every running deck,
+// (FP32 refinement) the refinement of the decks whose inner loop ended, and
+// the new block map with the loop condition.
+void launch_body(tl_batch *b, int ir, cudaGraphConditionalHandle h, int set_cond) {
+  for (int parity = 0; parity < 2; ++parity) {
+    if (ir) {
+      k_batch_ir_w<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
+      k_batch_ir_ur<<<b->total_u, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
+    } else {
+      k_batch_w<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
+      k_batch_ur<<<b->total_u, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
+    }
+  }
+  if (ir) {
+    k_batch_refine_map<<<1, 256, 0, b->stream>>>(b->d_decks, b->d_map);
+    k_batch_ir_fold<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map);
+    k_batch_ir_halo<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map);
+    k_batch_ir_resid<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map);
+  }
+  k_batch_map<<<1, 256, 0, b->stream>>>(b->d_decks, b->d_map, h, set_cond, ir);
+}
+
+// The loop: the while-node graph, or (TEALEAF_GB300_LOOP=host, for
+// profilers, which cannot see kernels inside graphs that hold conditional
+// nodes) the same trips launched from the host in batches of eight until the
+// map reports no running deck.  Trips after the last deck finished find no
+// blocks assigned and return at once.
+int run_loop(tl_batch *b, int ir) {
+  const char *loop = getenv("TEALEAF_GB300_LOOP");
+  if (!(loop && !strcmp(loop, "host"))) {
+    BCK(cudaGraphLaunch(ir ? b->graph_ir : b->graph, b->stream));
+    return TL_OK;
+  }
+  for (;;) {
+    for (int t = 0; t < 8; ++t) launch_body(b, ir, 0, 0);
+    BCK(cudaGetLastError());
+    int active = 0;
+    BCK(cudaMemcpyAsync(&active, &b->d_map->active, sizeof active, cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    if (active == 0) return TL_OK;
+  }
+}
+
 int build_graph(tl_batch *b, int ir) {
   cudaGraph_t graph = nullptr;
   BCK(cudaGraphCreate(&graph, 0));
@@ -473,22 +518,7 @@ int build_graph(tl_batch *b, int ir) {
     cudaGraphDestroy(graph);
     return bfail(b, e, "cudaStreamBeginCaptureToGraph");
   }
-  for (int parity = 0; parity < 2; ++parity) {
-    if (ir) {
-      k_batch_ir_w<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
-      k_batch_ir_ur<<<b->total_u, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
-    } else {
-      k_batch_w<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
-      k_batch_ur<<<b->total_u, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
-    }
-  }
-  if (ir) {
-    k_batch_refine_map<<<1, 256, 0, b->stream>>>(b->d_decks, b->d_map);
-    k_batch_ir_fold<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map);
-    k_batch_ir_halo<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map);
-    k_batch_ir_resid<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map);
-  }
-  k_batch_map<<<1, 256, 0, b->stream>>>(b->d_decks, b->d_map, h, 1, ir);
+  launch_body(b, ir, h, 1);
   cudaError_t le = cudaGetLastError();
   cudaGraph_t captured = nullptr;
   e = cudaStreamEndCapture(b->stream, &captured);
@@ -669,7 +699,7 @@ int batch_solve_ir(tl_batch *b, const double *rx, const double *ry, const tl_par
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess && !b->graph_ir) rc = build_graph(b, 1);
   if (e == cudaSuccess && !rc) e = cudaEventRecord(b->ev0, b->stream);
-  if (e == cudaSuccess && !rc) e = cudaGraphLaunch(b->graph_ir, b->stream);
+  if (e == cudaSuccess && !rc) rc = run_loop(b, 1);
   if (e == cudaSuccess && !rc) e = cudaEventRecord(b->ev1, b->stream);
   if (e == cudaSuccess && !rc) e = cudaEventSynchronize(b->ev1);
   float ms = 0.f;
@@ -748,7 +778,7 @@ extern "C" int tl_batch_solve(tl_batch *b, const double *rx, const double *ry, c
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess && !b->graph) rc = build_graph(b, 0);
     if (e == cudaSuccess && !rc) e = cudaEventRecord(b->ev0, b->stream);
-    if (e == cudaSuccess && !rc) e = cudaGraphLaunch(b->graph, b->stream);
+    if (e == cudaSuccess && !rc) rc = run_loop(b, 0);
     if (e == cudaSuccess && !rc) e = cudaEventRecord(b->ev1, b->stream);
     if (e == cudaSuccess && !rc) e = cudaEventSynchronize(b->ev1);
     float ms = 0.f;
@@ -756,22 +786,33 @@ extern "C" int tl_batch_solve(tl_batch *b, const double *rx, const double *ry, c
     b->last_ms = ms;
     if (e != cudaSuccess) rc = bfail(b, e, "batch loop");
   }
-  // per deck: the last iteration's p! and the halo of u, p; the results
+  // per deck: the last iteration's p! and the halo of u, p; under the
+  // relative criterion the true residual u0 - A u measured as in the
+  // single-deck solve (the deck counts as converged only if it meets eps);
+  // the results
   for (int k = 0; k < n && !rc; ++k) {
     tl_ctx *ctx = b->ctx[k];
     rc = tl_read_scalars(ctx);
     if (rc) break;
-    const DevScalars &sc = *ctx->host_sc;
+    const int iters = ctx->host_sc->iter, conv = ctx->host_sc->converged;
+    const double err = ctx->host_sc->error, bb = ctx->host_sc->bb;
     if (prm->maxiters >= 1) {
-      const double *pcur = (sc.iter & 1) ? ctx->F.pb : ctx->F.p;
+      const double *pcur = (iters & 1) ? ctx->F.pb : ctx->F.p;
       launch_tl_p(ctx->stream, ctx->F, ctx->g, ctx->walk_ur64, pcur, ctx->F.p, 0);
       rc = tl_halo_update(ctx, 1, nullptr, -1, 1);
     }
-    results[k].iters = sc.iter;
-    results[k].cg_iters = sc.iter;
-    results[k].error = prm->maxiters >= 1 ? sc.error : ERROR_START;
-    results[k].converged = sc.converged;
-    results[k].rel_residual = -1.0;
+    double rel = -1.0;
+    if (!rc && prm->criterion == TL_CRIT_RELATIVE) {
+      launch_true_resid(ctx->stream, ctx->F, ctx->g, ctx->walk_exact, TL_MODE_TEALEAF, 0);
+      if ((rc = tl_read_scalars(ctx))) break;
+      const double tr = ctx->host_sc->red[0];
+      rel = bb > 0 ? sqrt(tr / bb) : sqrt(tr);
+    }
+    results[k].iters = iters;
+    results[k].cg_iters = iters;
+    results[k].error = prm->maxiters >= 1 ? err : ERROR_START;
+    results[k].converged = prm->criterion == TL_CRIT_RELATIVE ? (rel >= 0 && rel < prm->eps) : conv;
+    results[k].rel_residual = rel;
     results[k].launches = 0;
   }
   if (!rc) {

@@ -127,7 +127,8 @@ void launch_ppcg_inner(cudaStream_t st, const Fields &F, const Geom &g, const Wa
                        double *sddst, int pp, int last, int exact, int guard, cudaGraphConditionalHandle cond,
                        int set_cond);
 void launch_jacobi(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk, const double *usrc, double *udst,
-                   int guard);
+                   int guard, int exact);
+void launch_init_rdiag(cudaStream_t st, const Fields &F, const Geom &g);  // diag = 1 / (1 + sum k)
 void launch_jacobi_check(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk, const double *u, int guard,
                          cudaGraphConditionalHandle cond, int set_cond);
 void launch_norm_r(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk);

@@ -378,7 +378,6 @@ int tl_ir_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_resu
   res->converged = rel < p.eps;
   res->refinements = refinements;
   res->launches = (int)ctx->launches;
-  if (prm->warmstart) tl_warm_after(ctx, res, prm->warmstart);
   return TL_OK;
 }
 

@@ -343,7 +343,7 @@ struct OpIrSweep {
     float c0 = 0.f, c1 = 0.f;  // alpha (CG, PPCG update) / 1/theta; or the Chebyshev pair
     if (KIND == SWEEP_CG || KIND == SWEEP_PPCG_UPDATE) {
       c0 = (float)sc->alpha;
-      c1 = (float)sc->theta;
+      c1 = (float)(1.0 / sc->theta);
     } else if (KIND == SWEEP_CHEBY) {
       const int idx = min(sc->cheby_iters + 2, sc->maxiters + 1);
       c0 = (float)F.chebyalpha[idx];
@@ -393,7 +393,7 @@ struct OpIrSweep {
           if (KIND == SWEEP_CG || KIND == SWEEP_PPCG_UPDATE) {
             va[k] = fmaf(c0, sv, av);        // x + alpha p'
             vb[k] = fmaf(-c0, wv[k], bv);    // r - alpha w
-            vo[k] = vb[k] / c1;              // sd = r / theta
+            vo[k] = vb[k] * c1;              // sd = r / theta
             rr = vb[k];
           } else if (KIND == SWEEP_CHEBY) {
             const float r = av - wv[k];      // r0 - w

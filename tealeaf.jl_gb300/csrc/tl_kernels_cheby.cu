@@ -109,6 +109,8 @@ struct OpCheby {
 // ---------------------------------------------------------------------------
 
 // u += alpha p, r -= alpha w, then sd = r / theta (the inner sweeps' start).
+// The fused form multiplies by 1/theta, formed once per thread (a division
+// per cell made this pass division-bound), and moves column pairs as double2.
 template <bool EXACT>
 struct OpPpcgUR : NoSkip {
   Fields F;
@@ -121,6 +123,22 @@ struct OpPpcgUR : NoSkip {
     if (i0 >= g.nx) return;
     const int nc = i0 + 1 < g.nx ? 2 : 1;
     const double alpha = F.sc->alpha, theta = F.sc->theta;
+    if (!EXACT && nc == 2) {
+      const double rtheta = 1.0 / theta;
+      for (int j = j0; j < j1; ++j) {
+        const size_t c = g.at(i0, j);
+        const double2 pv = ld2(p + c), wv = ld2(F.w + c);
+        double2 uv = ld2(F.u + c), rv = ld2(F.r + c);
+        uv.x = fma(alpha, pv.x, uv.x);
+        uv.y = fma(alpha, pv.y, uv.y);
+        rv.x = fma(-alpha, wv.x, rv.x);
+        rv.y = fma(-alpha, wv.y, rv.y);
+        st2(F.u + c, uv);
+        st2(F.r + c, rv);
+        st2(sd + c, make_double2(rv.x * rtheta, rv.y * rtheta));
+      }
+      return;
+    }
     for (int j = j0; j < j1; ++j) {
       const size_t c = g.at(i0, j);
       for (int m = 0; m < nc; ++m) {
@@ -215,6 +233,11 @@ struct OpPpcgInner {
 
 // One sweep: r = u (interior, plus the depth-1 faces, which hold the
 // reflection of u), u' = (u0 + sum k u_nbr) / (1 + sum k), error = sum |u' - u|.
+// EXACT: the reference's operation order and the division.  Otherwise the
+// numerator is a chain of fused multiply-adds and the division is a product
+// with 1 / (1 + sum k), stored once per solve in `diag` (a division per cell
+// made the sweep division-bound).
+template <bool EXACT>
 struct OpJacobi {
   Fields F;
   Geom g;
@@ -226,30 +249,36 @@ struct OpJacobi {
   __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
     SrcField src;
     src.f = usrc;
-    march<false>(g, F.kx, F.ky, F.diag, src, i0, j0, j1,
-                 [&](int j, const Nbr &c0, const Nbr &c1, bool has1, double2) {
-                   const size_t c = g.at(i0, j);
-                   const Nbr *q[2] = {&c0, &c1};
-                   const int nc = has1 ? 2 : 1;
-                   for (int m = 0; m < nc; ++m) {
-                     const Nbr &t = *q[m];
-                     double num = dadd(F.u0[c + m], dmul(t.kx1, t.e));
-                     num = dadd(num, dmul(t.kx0, t.w));
-                     num = dadd(num, dmul(t.ky1, t.n));
-                     num = dadd(num, dmul(t.ky0, t.s));
-                     const double den = dadd(dadd(dadd(dadd(1.0, t.kx0), t.kx1), t.ky0), t.ky1);
-                     const double un = ddiv(num, den);
-                     udst[c + m] = un;
-                     F.r[c + m] = t.c;
-                     acc[0] = dadd(acc[0], fabs(dsub(un, t.c)));
-                     // r .= u copies u's depth-1 halo, the reflection of u
-                     const int i = i0 + m;
-                     if (i == 0) F.r[c + m - 1] = t.c;
-                     if (i == g.nx - 1) F.r[c + m + 1] = t.c;
-                     if (j == 0) F.r[c + m - g.pitch] = t.c;
-                     if (j == g.ny - 1) F.r[c + m + g.pitch] = t.c;
-                   }
-                 });
+    march<!EXACT>(g, F.kx, F.ky, F.diag, src, i0, j0, j1,
+                  [&](int j, const Nbr &c0, const Nbr &c1, bool has1, double2) {
+                    const size_t c = g.at(i0, j);
+                    const Nbr *q[2] = {&c0, &c1};
+                    const int nc = has1 ? 2 : 1;
+                    for (int m = 0; m < nc; ++m) {
+                      const Nbr &t = *q[m];
+                      double un;
+                      if (EXACT) {
+                        double num = dadd(F.u0[c + m], dmul(t.kx1, t.e));
+                        num = dadd(num, dmul(t.kx0, t.w));
+                        num = dadd(num, dmul(t.ky1, t.n));
+                        num = dadd(num, dmul(t.ky0, t.s));
+                        const double den = dadd(dadd(dadd(dadd(1.0, t.kx0), t.kx1), t.ky0), t.ky1);
+                        un = ddiv(num, den);
+                      } else {
+                        const double num = fma(t.ky0, t.s, fma(t.ky1, t.n, fma(t.kx0, t.w, fma(t.kx1, t.e, F.u0[c + m]))));
+                        un = num * t.dg;
+                      }
+                      udst[c + m] = un;
+                      F.r[c + m] = t.c;
+                      acc[0] = dadd(acc[0], fabs(dsub(un, t.c)));
+                      // r .= u copies u's depth-1 halo, the reflection of u
+                      const int i = i0 + m;
+                      if (i == 0) F.r[c + m - 1] = t.c;
+                      if (i == g.nx - 1) F.r[c + m + 1] = t.c;
+                      if (j == 0) F.r[c + m - g.pitch] = t.c;
+                      if (j == g.ny - 1) F.r[c + m + g.pitch] = t.c;
+                    }
+                  });
   }
   __device__ void fin(const double *tot) const {
     DevScalars *sc = F.sc;
@@ -355,10 +384,29 @@ void launch_ppcg_inner(cudaStream_t st, const Fields &F, const Geom &g, const Wa
 }
 
 void launch_jacobi(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk, const double *usrc, double *udst,
-                   int guard) {
-  OpJacobi op;
-  op.F = F; op.g = g; op.usrc = usrc; op.udst = udst; op.guard = guard;
-  launch_walk<1>(st, op, wk, g.ny);
+                   int guard, int exact) {
+  if (exact) {
+    OpJacobi<true> op;
+    op.F = F; op.g = g; op.usrc = usrc; op.udst = udst; op.guard = guard;
+    launch_walk<1>(st, op, wk, g.ny);
+  } else {
+    OpJacobi<false> op;
+    op.F = F; op.g = g; op.usrc = usrc; op.udst = udst; op.guard = guard;
+    launch_walk<1>(st, op, wk, g.ny);
+  }
+}
+
+// diag = 1 / (1 + kx[i+1] + kx[i] + ky[j+1] + ky[j]): the fused Jacobi sweep's reciprocal.
+__global__ void k_init_rdiag(Fields F, Geom g) {
+  const long long n = (long long)g.nx * g.ny;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const size_t c = g.at((int)(k % g.nx), (int)(k / g.nx));
+    F.diag[c] = 1.0 / (1.0 + F.kx[c + 1] + F.kx[c] + F.ky[c + g.pitch] + F.ky[c]);
+  }
+}
+
+void launch_init_rdiag(cudaStream_t st, const Fields &F, const Geom &g) {
+  k_init_rdiag<<<grid_for((long long)g.nx * g.ny), 256, 0, st>>>(F, g);
 }
 
 void launch_jacobi_check(cudaStream_t st, const Fields &F, const Geom &g, const Walk &wk, const double *u, int guard,

@@ -356,7 +356,6 @@ int tl_cg_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_resu
       res->converged = 1;
       res->rel_residual = rel0;
       res->launches = (int)ctx->launches;
-      if (prm->warmstart) tl_warm_after(ctx, res, prm->warmstart);
       return TL_OK;
     }
   }
@@ -394,7 +393,6 @@ int tl_cg_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_resu
   res->converged = ran && (prm->criterion == TL_CRIT_RELATIVE ? (rel >= 0 && rel < prm->eps) : sc.converged);
   res->rel_residual = rel;
   res->launches = (int)ctx->launches;
-  if (prm->warmstart) tl_warm_after(ctx, res, prm->warmstart);
   return TL_OK;
 }
 

@@ -241,12 +241,15 @@ int tl_record_solver_body(tl_ctx *ctx, int which, cudaGraphConditionalHandle h) 
       }
       break;
     }
-    case TL_GRAPH_JACOBI: {
-      const Walk &wk = ctx->walk_exact;
-      launch_jacobi(st, F, g, wk, F.u, F.ub, 0);
-      launch_jacobi_check(st, F, g, wk, F.ub, 0, h, 0);
-      launch_jacobi(st, F, g, wk, F.ub, F.u, 1);
-      launch_jacobi_check(st, F, g, wk, F.u, 1, h, 1);
+    case TL_GRAPH_JACOBI:
+    case TL_GRAPH_JACOBI_FAST: {
+      const int exact = which == TL_GRAPH_JACOBI;
+      const Walk &wk = exact ? ctx->walk_exact : ctx->walk_w64;
+      const Walk &wc = ctx->walk_exact;
+      launch_jacobi(st, F, g, wk, F.u, F.ub, 0, exact);
+      launch_jacobi_check(st, F, g, wc, F.ub, 0, h, 0);
+      launch_jacobi(st, F, g, wk, F.ub, F.u, 1, exact);
+      launch_jacobi_check(st, F, g, wc, F.u, 1, h, 1);
       break;
     }
     default:
@@ -485,6 +488,11 @@ int tl_jacobi_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_
   CKL();
   launch_init_coef(ctx->stream, ctx->F, g, rx, ry, 1, prm->coefficient);
   CKL();
+  const int exact = prm->exact || ctx->cfg.mode == TL_MODE_REFERENCE;
+  if (!exact) {
+    launch_init_rdiag(ctx->stream, ctx->F, g);
+    CKL();
+  }
   if (tl_copy_u(ctx)) return TL_ERR_CUDA;
   launch_copy_full(ctx->stream, ctx->F.r, ctx->F.u, g);  // r's corners and outer layers: the first r .= u
   CKL();
@@ -496,7 +504,7 @@ int tl_jacobi_solve(tl_ctx *ctx, double rx, double ry, const tl_params *prm, tl_
   CKL();
   ctx->last_solve_ms = 0.0;
   if (prm->maxiters >= 1) {
-    if ((rc = tl_run_graph(ctx, TL_GRAPH_JACOBI, &ctx->last_solve_ms))) return rc;
+    if ((rc = tl_run_graph(ctx, exact ? TL_GRAPH_JACOBI : TL_GRAPH_JACOBI_FAST, &ctx->last_solve_ms))) return rc;
   }
   if ((rc = tl_read_scalars(ctx))) return rc;
   if (ctx->host_sc->iter & 1) {

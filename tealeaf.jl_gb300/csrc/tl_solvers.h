@@ -14,6 +14,7 @@ enum {
   TL_GRAPH_PPCG_EXACT,       // two PPCG outer steps with their inner sweeps
   TL_GRAPH_PPCG_FAST,
   TL_GRAPH_JACOBI,           // two Jacobi sweeps with their every-50th residual checks
+  TL_GRAPH_JACOBI_FAST,      // the same with the fused sweep
   TL_NGRAPH
 };
 
@@ -91,11 +92,9 @@ int tl_ppcg32_run(tl_ctx *ctx, const tl_params *prm, double rr, int *refinements
 int tl_ir_bench_kernel(tl_ctx *ctx, int kernel, int reps, double *ms_per_launch);
 tl::Walk *tl_ir_walk(tl_ctx *ctx, int kernel);  // the FP32 kernels' layouts (kernel 2, 3)
 
-// learned warm start (tl_warm.cu): after init + copyu!, maybe replace the
-// plain start by the network's prediction; always records u^n for the next step.
+// warm start (tl_warm.cu): after init + copyu!, maybe replace the plain start
+// by the projected prediction; always records u^n for the next step.
 int tl_warm_try(tl_ctx *ctx, double rx, double ry, int warmstart, tl_result *res);
-// after the solve: the iteration guard
-void tl_warm_after(tl_ctx *ctx, const tl_result *res, int warmstart);
 void tl_release_warm(tl_ctx *ctx);
 
 #define CK(x)                                                     \

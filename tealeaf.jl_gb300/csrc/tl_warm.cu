@@ -1,11 +1,24 @@
-// tl_warm.cu -- the learned warm start inside CG.solve! (tealeaf mode, FP64
-// and FP32-refined CG).  After tea_leaf_init and copyu! the context holds
-// u = u0 = u^n and the plain start's residual r = p = u0 - A u^n.  With the
-// previous step's u^{n-1} kept on the device, the network predicts
-// x = u^n + (1 + g) (u^n - u^{n-1}); the plain start is both the fallback and
-// the judge: x replaces u (and its residual replaces r, p) only when
-// ||u0 - A x|| < ||u0 - A u^n||.  The solve then runs unchanged and must meet
-// eps on the true residual as before.
+// tl_warm.cu -- the warm start inside CG.solve! (tealeaf mode, FP64 and
+// FP32-refined CG).  After tea_leaf_init and copyu! the context holds
+// u = u0 = u^n and the plain start's residual r = p = u0 - A u^n.  The
+// context keeps the last three solutions u^{n-1}, u^{n-2}, u^{n-3}.
+//
+// The candidate start is the A-norm projection of the solution u^{n+1} =
+// A^{-1} u0 onto a small basis: u^n, the increments u^n - u^{n-1},
+// u^{n-1} - u^{n-2}, u^{n-2} - u^{n-3} (those that exist), and, with the
+// network, the network's correction g (u^n - u^{n-1}) (its prediction is
+// u^n + (1 + g)(u^n - u^{n-1})).  With V the basis, the start
+// x = V c minimises ||x - A^{-1} u0||_A over the span, from the Gram system
+// (V^T A V) c = V^T u0: one pass over the fields forms every A v_j on the fly
+// and the m(m+1)/2 + m sums, the host solves the m x m system (m <= 5), and a
+// second pass forms x.  The span holds the plain start u^n and the linear
+// extrapolation 2u^n - u^{n-1}, so x is never farther from the solution in
+// the A-norm than either; the network's term enters with the weight that
+// serves that norm best, and with weight ~0 where it does not help.
+//
+// The plain start is both the fallback and the judge: x replaces u (and its
+// residual replaces r, p) only when ||u0 - A x|| < ||u0 - A u^n||.  The solve
+// then runs unchanged and must meet eps on the true residual as before.
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -24,16 +37,13 @@ struct tl_warm_state {
   void *act = nullptr;                  // feature map (16 ch) + two 32-channel activation maps + g
   __nv_bfloat16 *feat = nullptr, *a0 = nullptr, *a1 = nullptr;
   float *g = nullptr;
-  double *uprev = nullptr;              // u^{n-1}, laid out like the context's fields
+  double *hist[3] = {};                 // u^{n-1}, u^{n-2}, u^{n-3}, laid out like the context's fields
+  int nhist = 0;                        // how many of them hold an earlier step
+  int net_skip = 0;                     // steps left before the network runs again
+  int net_backoff = 1;                  // steps the next loss of the network's term skips (1, 2, ... 32)
   double *stats = nullptr;              // block partials of u.u and d.d, then the two totals
+  double *gram = nullptr;               // block partials of the Gram system, then its totals
   tl_warm_crop *crop = nullptr;         // device copy of the whole-domain crop
-  int have_prev = 0;
-  // the iteration guard (tl_warm_after): plain-start control solves bracket
-  // runs of at most `trust` solves from the prediction
-  int ctrl_iters = -1;                  // iterations of the last solve from the plain start
-  int run = 0;                          // solves from the prediction since that control
-  long long run_iters = 0;              // their iterations
-  int trust = 2, cooloff = 0, backoff = 4;
 };
 
 namespace tl {
@@ -78,33 +88,140 @@ __global__ void k_warm_stats_fold(double *part, int nblk) {
   part[2 * nblk + 1] = sd;
 }
 
-// x = u0 + (1 + g) (u0 - uprev) on the interior, into ub.
-__global__ void k_warm_candidate(Fields F, Geom g, const double *uprev, const float *gv) {
+// The projection basis at one cell: v0 = u^n, then the increments
+// u^n - u^{n-1}, u^{n-1} - u^{n-2}, u^{n-2} - u^{n-3} (nh of them), then the
+// network's correction g (u^n - u^{n-1}) when `gv` is set.
+constexpr int PROJ_MAX = 5;
+constexpr int PROJ_NG = PROJ_MAX * (PROJ_MAX + 1) / 2;  // upper triangle of V^T A V
+constexpr int PROJ_NACC = PROJ_NG + PROJ_MAX;           // ... then V^T u0
+constexpr int GRAM_BLOCKS = 304;
+
+struct ProjBasis {
+  const double *u0, *h0, *h1, *h2;  // u^n, u^{n-1}, u^{n-2}, u^{n-3}
+  const float *gv;                  // network output g (interior, row-major), or null
+  int nh;                           // increments in the basis (1..3)
+  int m;                            // basis size: 1 + nh + (gv != null)
+};
+
+__device__ __forceinline__ void basis_at(const ProjBasis &B, size_t c, long long k, double (&v)[PROJ_MAX]) {
+  const double u = B.u0[c], a = B.h0[c];
+  const double b = B.nh >= 2 ? B.h1[c] : 0.0, e = B.nh >= 3 ? B.h2[c] : 0.0;
+  const double net = B.gv ? (double)B.gv[k] * (u - a) : 0.0;
+  v[0] = u;
+  v[1] = u - a;
+  v[2] = B.nh >= 2 ? a - b : net;
+  v[3] = B.nh >= 3 ? b - e : (B.nh == 2 ? net : 0.0);
+  v[4] = B.nh >= 3 ? net : 0.0;
+}
+
+// One pass: A v_j at every interior cell for every basis vector (the
+// 5-point operator in difference form, v + sum k (v - v_nbr), with the
+// reflective boundary folded in: a neighbour across the edge is the cell
+// itself), and the sums v_a . A v_b (a <= b) and v_a . u0.  Fixed grid and
+// block order: the sums are deterministic.
+__global__ void __launch_bounds__(256) k_warm_gram(Fields F, Geom g, ProjBasis B, double *part) {
+  double acc[PROJ_NACC];
+#pragma unroll
+  for (int a = 0; a < PROJ_NACC; ++a) acc[a] = 0.0;
+  const int m = B.m;
   const long long n = (long long)g.nx * g.ny;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(k % g.nx), j = (int)(k / g.nx);
     const size_t c = g.at(i, j);
-    const double u = F.u0[c];
-    F.ub[c] = u + (1.0 + (double)gv[k]) * (u - uprev[c]);
+    const size_t cE = i + 1 < g.nx ? c + 1 : c, cW = i > 0 ? c - 1 : c;
+    const size_t cN = j + 1 < g.ny ? c + g.pitch : c, cS = j > 0 ? c - g.pitch : c;
+    const long long kE = i + 1 < g.nx ? k + 1 : k, kW = i > 0 ? k - 1 : k;
+    const long long kN = j + 1 < g.ny ? k + g.nx : k, kS = j > 0 ? k - g.nx : k;
+    double vc[PROJ_MAX] = {}, vE[PROJ_MAX] = {}, vW[PROJ_MAX] = {}, vN[PROJ_MAX] = {}, vS[PROJ_MAX] = {};
+    basis_at(B, c, k, vc);
+    basis_at(B, cE, kE, vE);
+    basis_at(B, cW, kW, vW);
+    basis_at(B, cN, kN, vN);
+    basis_at(B, cS, kS, vS);
+    const double kxE = F.kx[c + 1], kxW = F.kx[c], kyN = F.ky[c + g.pitch], kyS = F.ky[c];
+    double av[PROJ_MAX];
+#pragma unroll
+    for (int b = 0; b < PROJ_MAX; ++b)
+      av[b] = vc[b] + kxE * (vc[b] - vE[b]) + kxW * (vc[b] - vW[b]) + kyN * (vc[b] - vN[b]) + kyS * (vc[b] - vS[b]);
+    int t = 0;
+#pragma unroll
+    for (int a = 0; a < PROJ_MAX; ++a)
+#pragma unroll
+      for (int b = a; b < PROJ_MAX; ++b, ++t)
+        if (b < m) acc[t] = fma(vc[a], av[b], acc[t]);
+#pragma unroll
+    for (int a = 0; a < PROJ_MAX; ++a)
+      if (a < m) acc[PROJ_NG + a] = fma(vc[a], vc[0], acc[PROJ_NG + a]);
+  }
+  __shared__ double ws[8][PROJ_NACC];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int a = 0; a < PROJ_NACC; ++a) {
+    const double v = warp_butterfly(acc[a]);
+    if (lane == 0) ws[warp][a] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < PROJ_NACC) {
+    double v = ws[0][threadIdx.x];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v += ws[w][threadIdx.x];
+    part[(size_t)blockIdx.x * PROJ_NACC + threadIdx.x] = v;
   }
 }
 
-__global__ void k_copy_u0(Fields F, Geom g, double *uprev) {
+__global__ void k_warm_gram_fold(double *part, int nblk) {
+  if (threadIdx.x >= PROJ_NACC) return;
+  double v = 0.0;
+  for (int b = 0; b < nblk; ++b) v += part[(size_t)b * PROJ_NACC + threadIdx.x];
+  part[(size_t)nblk * PROJ_NACC + threadIdx.x] = v;
+}
+
+struct ProjCoef {
+  double c[PROJ_MAX];
+};
+
+// x = V c on the interior, into ub.
+__global__ void k_warm_combine(Fields F, Geom g, ProjBasis B, ProjCoef C) {
   const long long n = (long long)g.nx * g.ny;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
     const size_t c = g.at((int)(k % g.nx), (int)(k / g.nx));
-    uprev[c] = F.u0[c];
+    double v[PROJ_MAX] = {};
+    basis_at(B, c, k, v);
+    double x = 0.0;
+#pragma unroll
+    for (int a = 0; a < PROJ_MAX; ++a)
+      if (a < B.m) x = fma(C.c[a], v[a], x);
+    F.ub[c] = x;
   }
 }
 
-// Residual of the candidate: w = u0 - A ub (true residual, 5-point operator), sum w.w.
+// x = 2 u^n - u^{n-1} on the interior, into ub.
+__global__ void k_warm_extrapolate(Fields F, Geom g, const double *h0) {
+  const long long n = (long long)g.nx * g.ny;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const size_t c = g.at((int)(k % g.nx), (int)(k / g.nx));
+    const double u = F.u0[c];
+    F.ub[c] = u + (u - h0[c]);
+  }
+}
+
+__global__ void k_copy_u0(Fields F, Geom g, double *dst) {
+  const long long n = (long long)g.nx * g.ny;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const size_t c = g.at((int)(k % g.nx), (int)(k / g.nx));
+    dst[c] = F.u0[c];
+  }
+}
+
+// Residual of the candidate: w = u0 - A ub (true residual, 5-point operator), sum w.w;
+// with write 0 only the sum.
 struct OpWarmResid : NoSkip {
   Fields F;
   Geom g;
+  int write;  // 0: the norm only
   __device__ void cell(int i, int j, double (&acc)[1]) const {
     const size_t c = g.at(i, j);
     const double t = dsub(F.u0[c], smvp_exact(F, g, F.ub, c, TL_MODE_TEALEAF));
-    F.w[c] = t;
+    if (write) F.w[c] = t;
     acc[0] = dadd(acc[0], dmul(t, t));
   }
   __device__ void tile(int i0, int j0, int j1, double (&acc)[1]) const {
@@ -148,7 +265,7 @@ void tl_release_warm(tl_ctx *ctx) {
   if (!ws) return;
   if (ws->wbuf) cudaFree(ws->wbuf);
   if (ws->act) cudaFree(ws->act);
-  if (ws->uprev) cudaFree(ws->uprev);
+  if (ws->hist[0]) cudaFree(ws->hist[0]);  // one allocation holds the three
   if (ws->stats) cudaFree(ws->stats);
   if (ws->crop) cudaFree(ws->crop);
   delete ws;
@@ -203,39 +320,198 @@ extern "C" int tl_warm_load(tl_ctx *ctx, const float *params, int nparams) {
 extern "C" int tl_warm_reset(tl_ctx *ctx) {
   if (!ctx) return TL_ERR_ARG;
   if (tl_warm_state *ws = ctx->warm) {
-    ws->have_prev = 0;
-    ws->ctrl_iters = -1;
-    ws->run = 0;
-    ws->run_iters = 0;
-    ws->trust = 2;
-    ws->cooloff = 0;
-    ws->backoff = 4;
+    ws->nhist = 0;
+    ws->net_skip = 0;
+    ws->net_backoff = 1;
   }
   return TL_OK;
 }
 
-static int ensure_warm_buffers(tl_ctx *ctx) {
+// Buffers of every warm-start mode: the three earlier solutions, the sums;
+// the network's feature and activation maps only when `network`.
+static int ensure_warm_buffers(tl_ctx *ctx, int network) {
   tl_warm_state *ws = ctx->warm;
   const Geom &g = ctx->g;
-  if (ws->act) return TL_OK;
   const size_t cells = (size_t)g.nx * g.ny;
-  const size_t fbytes = (cells * 16 * 2 + 255) / 256 * 256, abytes = (cells * 32 * 2 + 255) / 256 * 256;
-  CK(cudaMalloc(&ws->act, fbytes + 2 * abytes + sizeof(float) * cells));
-  char *base = static_cast<char *>(ws->act);
-  ws->feat = reinterpret_cast<__nv_bfloat16 *>(base);
-  ws->a0 = reinterpret_cast<__nv_bfloat16 *>(base + fbytes);
-  ws->a1 = reinterpret_cast<__nv_bfloat16 *>(base + fbytes + abytes);
-  ws->g = reinterpret_cast<float *>(base + fbytes + 2 * abytes);
-  CK(cudaMalloc(&ws->uprev, sizeof(double) * (size_t)g.pitch * g.Y));
-  CK(cudaMemsetAsync(ws->uprev, 0, sizeof(double) * (size_t)g.pitch * g.Y, ctx->stream));
-  CK(cudaMalloc(&ws->stats, sizeof(double) * (2 * STAT_BLOCKS + 2)));
-  CK(cudaMalloc(&ws->crop, sizeof(tl_warm_crop)));
+  if (!ws->hist[0]) {
+    const size_t fb = sizeof(double) * (size_t)g.pitch * g.Y;
+    double *h = nullptr;
+    CK(cudaMalloc(&h, 3 * fb));
+    CK(cudaMemsetAsync(h, 0, 3 * fb, ctx->stream));
+    for (int k = 0; k < 3; ++k) ws->hist[k] = h + (size_t)k * g.pitch * g.Y;
+    CK(cudaMalloc(&ws->stats, sizeof(double) * (2 * STAT_BLOCKS + 2 + (size_t)(GRAM_BLOCKS + 1) * PROJ_NACC)));
+    ws->gram = ws->stats + 2 * STAT_BLOCKS + 2;
+    CK(cudaMalloc(&ws->crop, sizeof(tl_warm_crop)));
+  }
+  if (network && !ws->act) {
+    const size_t fbytes = (cells * 16 * 2 + 255) / 256 * 256, abytes = (cells * 32 * 2 + 255) / 256 * 256;
+    CK(cudaMalloc(&ws->act, fbytes + 2 * abytes + sizeof(float) * cells));
+    char *base = static_cast<char *>(ws->act);
+    ws->feat = reinterpret_cast<__nv_bfloat16 *>(base);
+    ws->a0 = reinterpret_cast<__nv_bfloat16 *>(base + fbytes);
+    ws->a1 = reinterpret_cast<__nv_bfloat16 *>(base + fbytes + abytes);
+    ws->g = reinterpret_cast<float *>(base + fbytes + 2 * abytes);
+  }
+  return TL_OK;
+}
+
+// The network's output g for the current step (features from u^n, the
+// density and u^n - u^{n-1}, then the six convolutions).
+static int run_network(tl_ctx *ctx, double rx, double ry) {
+  tl_warm_state *ws = ctx->warm;
+  const Geom &g = ctx->g;
+  const Fields &F = ctx->F;
+  cudaStream_t st = ctx->stream;
+  k_warm_stats<<<STAT_BLOCKS, 256, 0, st>>>(F, g, ws->hist[0], ws->stats);
+  k_warm_stats_fold<<<1, 1, 0, st>>>(ws->stats, STAT_BLOCKS);
+  CKL();
+  double tot[2];
+  CK(cudaMemcpyAsync(tot, ws->stats + 2 * STAT_BLOCKS, sizeof tot, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  ctx->launches += 2;
+  if (!(tot[0] > 0) || !(tot[1] > 0)) return 1;  // no increment: nothing for the network to scale
+  const double cells = (double)g.nx * g.ny;
+  tl_warm_crop cr{};
+  cr.u = F.u0 + g.at(0, 0);
+  cr.uprev = ws->hist[0] + g.at(0, 0);
+  cr.rho = F.density + g.at(0, 0);
+  cr.pitch = g.pitch;
+  cr.nx = g.nx;
+  cr.ny = g.ny;
+  cr.rx = rx;
+  cr.ry = ry;
+  cr.inv_su = 1.0 / sqrt(tot[0] / cells);
+  cr.inv_sd = 1.0 / sqrt(tot[1] / cells);
+  CK(cudaMemcpyAsync(ws->crop, &cr, sizeof cr, cudaMemcpyHostToDevice, st));
+  int rc = tl_warm_features_launch(ws->crop, 1, g.ny, g.nx, ws->feat, st);
+  if (rc) {
+    tl_set_error(ctx, "warm-start feature kernel failed to launch");
+    return -rc;
+  }
+  const __nv_bfloat16 *in = ws->feat;
+  __nv_bfloat16 *bufs[2] = {ws->a0, ws->a1};
+  for (int l = 0; l < TL_WARM_LAYERS; ++l) {
+    const int last = l == TL_WARM_LAYERS - 1;
+    __nv_bfloat16 *out = last ? nullptr : bufs[l & 1];
+    rc = tl_conv_forward(in, ws->w[l], ws->b[l], nullptr, nullptr, out, last ? ws->g : nullptr, 1, g.ny, g.nx,
+                         TL_WARM_CIN[l], TL_WARM_COUT[l], last ? 0 : 1, st);
+    if (rc) {
+      tl_set_error(ctx, "warm-start convolution %d failed to launch", l);
+      return -rc;
+    }
+    in = out;
+  }
+  ctx->launches += 1 + TL_WARM_LAYERS;
+  return 0;
+}
+
+// Solves the m x m Gram system G c = h (symmetric, positive semi-definite)
+// on the host: the basis is scaled to unit A-norm, the scaled matrix is
+// diagonalised by cyclic Jacobi rotations, and directions whose eigenvalue is
+// below 1e-12 of the largest are dropped (nearly dependent increments).
+// Returns 0 when no usable solution exists.
+static int solve_gram(int m, const double *G, const double *h, double *c) {
+  double S[PROJ_MAX][PROJ_MAX], Q[PROJ_MAX][PROJ_MAX], sc[PROJ_MAX], hs[PROJ_MAX];
+  for (int a = 0; a < m; ++a) {
+    if (!(G[a * PROJ_MAX + a] > 0) || !std::isfinite(G[a * PROJ_MAX + a])) return 0;
+    sc[a] = 1.0 / std::sqrt(G[a * PROJ_MAX + a]);
+  }
+  for (int a = 0; a < m; ++a) {
+    hs[a] = sc[a] * h[a];
+    for (int b = 0; b < m; ++b) {
+      S[a][b] = sc[a] * G[a * PROJ_MAX + b] * sc[b];
+      Q[a][b] = a == b ? 1.0 : 0.0;
+    }
+  }
+  for (int sweep = 0; sweep < 64; ++sweep) {
+    double off = 0.0;
+    for (int a = 0; a < m; ++a)
+      for (int b = a + 1; b < m; ++b) off += S[a][b] * S[a][b];
+    if (off < 1e-30) break;
+    for (int p = 0; p < m; ++p)
+      for (int q = p + 1; q < m; ++q) {
+        if (std::fabs(S[p][q]) < 1e-300) continue;
+        const double theta = 0.5 * (S[q][q] - S[p][p]) / S[p][q];
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double cs = 1.0 / std::sqrt(t * t + 1.0), sn = t * cs;
+        for (int k = 0; k < m; ++k) {  // columns p, q of S
+          const double skp = S[k][p], skq = S[k][q];
+          S[k][p] = cs * skp - sn * skq;
+          S[k][q] = sn * skp + cs * skq;
+        }
+        for (int k = 0; k < m; ++k) {  // rows p, q
+          const double spk = S[p][k], sqk = S[q][k];
+          S[p][k] = cs * spk - sn * sqk;
+          S[q][k] = sn * spk + cs * sqk;
+        }
+        for (int k = 0; k < m; ++k) {
+          const double qkp = Q[k][p], qkq = Q[k][q];
+          Q[k][p] = cs * qkp - sn * qkq;
+          Q[k][q] = sn * qkp + cs * qkq;
+        }
+      }
+  }
+  double lmax = 0.0;
+  for (int a = 0; a < m; ++a) lmax = std::fmax(lmax, S[a][a]);
+  if (!(lmax > 0) || !std::isfinite(lmax)) return 0;
+  double y[PROJ_MAX] = {};
+  for (int e = 0; e < m; ++e) {
+    const double lam = S[e][e];
+    if (!(lam > 1e-12 * lmax)) continue;
+    double qh = 0.0;
+    for (int a = 0; a < m; ++a) qh += Q[a][e] * hs[a];
+    for (int a = 0; a < m; ++a) y[a] += Q[a][e] * qh / lam;
+  }
+  for (int a = 0; a < m; ++a) {
+    c[a] = sc[a] * y[a];
+    if (!std::isfinite(c[a])) return 0;
+  }
+  return 1;
+}
+
+// x = V c into ub, its halo, and ||u0 - A x||^2 (with `write`, the residual
+// itself into w for accept_candidate).
+static int candidate_residual(tl_ctx *ctx, const ProjBasis &B, const ProjCoef &C, int write, double *rr) {
+  const Geom &g = ctx->g;
+  const Fields &F = ctx->F;
+  cudaStream_t st = ctx->stream;
+  k_warm_combine<<<grid_cells(g), 256, 0, st>>>(F, g, B, C);
+  CKL();
+  double *ub = F.ub;
+  launch_halo(st, &ub, 1, g, 1, TL_MODE_TEALEAF);
+  CKL();
+  OpWarmResid op;
+  op.F = F;
+  op.g = g;
+  op.write = write;
+  launch_walk<1>(st, op, ctx->walk_exact, g.ny);
+  CKL();
+  ctx->launches += 3;
+  int rc = tl_read_scalars(ctx);
+  if (rc) return rc;
+  *rr = ctx->host_sc->red[0];
+  return TL_OK;
+}
+
+// The candidate in ub (its residual in w) becomes the start: u = ub,
+// r = p = w, rr = its r.r, and the halo of u, p.
+static int accept_candidate(tl_ctx *ctx) {
+  const Geom &g = ctx->g;
+  const Fields &F = ctx->F;
+  cudaStream_t st = ctx->stream;
+  launch_copy_full(st, F.u, F.ub, g);
+  k_warm_accept<<<grid_cells(g), 256, 0, st>>>(F, g);
+  CKL();
+  const int up[2] = {TL_EX_U, TL_EX_P};
+  int rc = tl_halo_update(ctx, 1, up, 2, 1);
+  if (rc) return rc;
+  ctx->launches += 3;
   return TL_OK;
 }
 
 // Called by the CG solves after tea_leaf_init, the halo and copyu!.
 int tl_warm_try(tl_ctx *ctx, double rx, double ry, int warmstart, tl_result *res) {
-  if (warmstart != TL_WARM_NETWORK && warmstart != TL_WARM_EXTRAPOLATE) {
+  if (warmstart != TL_WARM_NETWORK && warmstart != TL_WARM_EXTRAPOLATE && warmstart != TL_WARM_HISTORY) {
     tl_set_error(ctx, "unknown warm-start mode %d", warmstart);
     return TL_ERR_ARG;
   }
@@ -248,11 +524,12 @@ int tl_warm_try(tl_ctx *ctx, double rx, double ry, int warmstart, tl_result *res
     if (!ctx->warm) return TL_ERR_NOMEM;
   }
   tl_warm_state *ws = ctx->warm;
-  if (warmstart == TL_WARM_NETWORK && !ws->wbuf) {
+  const int network = warmstart == TL_WARM_NETWORK;
+  if (network && !ws->wbuf) {
     tl_set_error(ctx, "warm start asked before tl_warm_load");
     return TL_ERR_STATE;
   }
-  int rc = ensure_warm_buffers(ctx);
+  int rc = ensure_warm_buffers(ctx, network);
   if (rc) return rc;
   const Geom &g = ctx->g;
   const Fields &F = ctx->F;
@@ -262,127 +539,117 @@ int tl_warm_try(tl_ctx *ctx, double rx, double ry, int warmstart, tl_result *res
   res->r0_plain = bb > 0 ? sqrt(rr_plain / bb) : sqrt(rr_plain);
   res->r0_pred = -1.0;
   res->warm = 0;
-  const int extrapolate = warmstart == TL_WARM_EXTRAPOLATE;
-  if (ws->have_prev && ws->cooloff > 0) {
-    --ws->cooloff;
-    res->warm = 3;
-  } else if (ws->have_prev && (ws->ctrl_iters < 0 || ws->run >= ws->trust)) {
-    res->warm = 4;  // control solve from the plain start
-  } else if (ws->have_prev) {
-    k_warm_stats<<<STAT_BLOCKS, 256, 0, st>>>(F, g, ws->uprev, ws->stats);
-    k_warm_stats_fold<<<1, 1, 0, st>>>(ws->stats, STAT_BLOCKS);
+  for (int a = 0; a < 5; ++a) res->warm_coef[a] = 0.0;
+  if (ws->nhist >= 1 && warmstart == TL_WARM_EXTRAPOLATE) {
+    k_warm_extrapolate<<<grid_cells(g), 256, 0, st>>>(F, g, ws->hist[0]);
     CKL();
-    double tot[2];
-    CK(cudaMemcpyAsync(tot, ws->stats + 2 * STAT_BLOCKS, sizeof tot, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
+    ctx->launches += 1;
+    res->warm_coef[0] = 2.0;
+    res->warm_coef[1] = -1.0;
+  } else if (ws->nhist >= 1) {
+    ProjBasis B;
+    B.u0 = F.u0;
+    B.h0 = ws->hist[0];
+    B.h1 = ws->hist[1];
+    B.h2 = ws->hist[2];
+    B.nh = ws->nhist;
+    B.gv = nullptr;
+    if (network && ws->net_skip > 0) {
+      --ws->net_skip;  // backing off after the network's term lost its judge
+    } else if (network) {
+      const int nrc = run_network(ctx, rx, ry);
+      if (nrc < 0) return -nrc;
+      if (nrc == 0) B.gv = ws->g;
+    }
+    B.m = 1 + B.nh + (B.gv ? 1 : 0);
+    k_warm_gram<<<GRAM_BLOCKS, 256, 0, st>>>(F, g, B, ws->gram);
+    k_warm_gram_fold<<<1, 32, 0, st>>>(ws->gram, GRAM_BLOCKS);
+    CKL();
     ctx->launches += 2;
-    const double cells = (double)g.nx * g.ny;
-    if (tot[0] > 0 && tot[1] > 0) {
-      tl_warm_crop cr{};
-      cr.u = F.u0 + g.at(0, 0);
-      cr.uprev = ws->uprev + g.at(0, 0);
-      cr.rho = F.density + g.at(0, 0);
-      cr.pitch = g.pitch;
-      cr.nx = g.nx;
-      cr.ny = g.ny;
-      cr.rx = rx;
-      cr.ry = ry;
-      cr.inv_su = 1.0 / sqrt(tot[0] / cells);
-      cr.inv_sd = 1.0 / sqrt(tot[1] / cells);
-      CK(cudaMemcpyAsync(ws->crop, &cr, sizeof cr, cudaMemcpyHostToDevice, st));
-      if (extrapolate) {
-        CK(cudaMemsetAsync(ws->g, 0, sizeof(float) * (size_t)g.nx * g.ny, st));   // g = 0: u^n + (u^n - u^{n-1})
+    double tot[PROJ_NACC];
+    CK(cudaMemcpyAsync(tot, ws->gram + (size_t)GRAM_BLOCKS * PROJ_NACC, sizeof tot, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    double G[PROJ_MAX * PROJ_MAX] = {}, h[PROJ_MAX] = {};
+    for (int a = 0, t = 0; a < PROJ_MAX; ++a)
+      for (int b = a; b < PROJ_MAX; ++b, ++t) G[a * PROJ_MAX + b] = G[b * PROJ_MAX + a] = tot[t];
+    for (int a = 0; a < PROJ_MAX; ++a) h[a] = tot[PROJ_NG + a];
+    // the history-only projection (the leading block of the system), and
+    // with the network the full one; the network's term is kept only when
+    // its candidate's residual is below the history-only candidate's
+    ProjCoef Ch{}, Cn{};
+    const int mh = 1 + B.nh;
+    const int okh = solve_gram(mh, G, h, Ch.c);
+    const int okn = B.gv ? solve_gram(B.m, G, h, Cn.c) : 0;
+    const ProjCoef *chosen = nullptr;
+    if (okh && okn) {
+      ProjBasis Bh = B;
+      Bh.m = mh;
+      double rr_h = 0.0, rr_n = 0.0;
+      if ((rc = candidate_residual(ctx, Bh, Ch, 0, &rr_h))) return rc;
+      if ((rc = candidate_residual(ctx, B, Cn, 0, &rr_n))) return rc;
+      if (rr_n < rr_h) {
+        chosen = &Cn;
+        res->warm = 1;
+        ws->net_backoff = 1;
       } else {
-        if ((rc = tl_warm_features_launch(ws->crop, 1, g.ny, g.nx, ws->feat, st))) {
-          tl_set_error(ctx, "warm-start feature kernel failed to launch");
-          return rc;
-        }
-        const __nv_bfloat16 *in = ws->feat;
-        __nv_bfloat16 *bufs[2] = {ws->a0, ws->a1};
-        for (int l = 0; l < TL_WARM_LAYERS; ++l) {
-          const int last = l == TL_WARM_LAYERS - 1;
-          __nv_bfloat16 *out = last ? nullptr : bufs[l & 1];
-          rc = tl_conv_forward(in, ws->w[l], ws->b[l], nullptr, nullptr, out, last ? ws->g : nullptr, 1, g.ny,
-                               g.nx, TL_WARM_CIN[l], TL_WARM_COUT[l], last ? 0 : 1, st);
-          if (rc) {
-            tl_set_error(ctx, "warm-start convolution %d failed to launch", l);
-            return rc;
-          }
-          in = out;
-        }
-        ctx->launches += 1 + TL_WARM_LAYERS;
+        // the network's term did not pay: skip the next 1, 2, 4, ... 32 inferences
+        chosen = &Ch;
+        B.m = mh;
+        res->warm = 3;
+        ws->net_skip = ws->net_backoff;
+        ws->net_backoff = ws->net_backoff < 32 ? 2 * ws->net_backoff : 32;
       }
-      k_warm_candidate<<<grid_cells(g), 256, 0, st>>>(F, g, ws->uprev, ws->g);
-      CKL();
-      double *ub = F.ub;
-      launch_halo(st, &ub, 1, g, 1, TL_MODE_TEALEAF);
-      CKL();
-      OpWarmResid op;
-      op.F = F;
-      op.g = g;
-      launch_walk<1>(st, op, ctx->walk_exact, g.ny);
-      CKL();
-      ctx->launches += 3;
-      if ((rc = tl_read_scalars(ctx))) return rc;
-      const double rr_pred = ctx->host_sc->red[0];
+    } else if (okh) {
+      chosen = &Ch;
+      B.m = mh;
+      res->warm = network ? 3 : 1;
+    }
+    if (chosen) {
+      double rr_pred = 0.0;
+      if ((rc = candidate_residual(ctx, B, *chosen, 1, &rr_pred))) return rc;
+      const double *cc = chosen->c;
+      res->warm_coef[0] = cc[0] + cc[1];
+      res->warm_coef[1] = (B.nh >= 2 ? cc[2] : 0.0) - cc[1];
+      res->warm_coef[2] = (B.nh >= 3 ? cc[3] : 0.0) - (B.nh >= 2 ? cc[2] : 0.0);
+      res->warm_coef[3] = B.nh >= 3 ? -cc[3] : 0.0;
+      res->warm_coef[4] = B.m > mh ? cc[mh] : 0.0;
       res->r0_pred = bb > 0 ? sqrt(rr_pred / bb) : sqrt(rr_pred);
       if (rr_pred < rr_plain) {
-        launch_copy_full(st, F.u, F.ub, g);
-        k_warm_accept<<<grid_cells(g), 256, 0, st>>>(F, g);
-        CKL();
-        const int up[2] = {TL_EX_U, TL_EX_P};
-        if ((rc = tl_halo_update(ctx, 1, up, 2, 1))) return rc;
-        ctx->launches += 3;
-        res->warm = 1;
+        if ((rc = accept_candidate(ctx))) return rc;
       } else {
         res->warm = 2;
       }
     }
   }
-  k_copy_u0<<<grid_cells(g), 256, 0, st>>>(F, g, ws->uprev);
-  CKL();
-  ctx->launches += 1;
-  ws->have_prev = 1;
-  return TL_OK;
-}
-
-// After the solve: the second judgement.  A smaller initial residual does
-// not imply fewer CG iterations (error the prediction adds across the whole
-// spectrum costs more than the smooth error of the plain start), so runs of at
-// most `trust` solves from the prediction are bracketed by control solves
-// from the plain start.  When a run's mean iteration count exceeds the mean of
-// its two controls, the prediction pauses for `backoff` steps (4, 8, ... 64)
-// and trust drops to 2; otherwise trust doubles (up to 32) and the backoff
-// returns to 4.  A network prediction rejected by the residual judge
-// (outside a run) pauses the next ones the same way, so that rejected
-// inference stops costing time.
-void tl_warm_after(tl_ctx *ctx, const tl_result *res, int warmstart) {
-  tl_warm_state *ws = ctx->warm;
-  if (!ws) return;
-  if (res->warm == 1) {
-    ++ws->run;
-    ws->run_iters += res->iters;
-    return;
-  }
-  if (res->warm == 2 && ws->run == 0 && warmstart == TL_WARM_NETWORK) {
-    // the network's prediction lost to the plain start by residual: its
-    // inference was wasted, so the next attempts back off the same way (the
-    // extrapolation candidate costs one pass and is tried every step)
-    ws->cooloff = ws->backoff;
-    ws->backoff = ws->backoff < 64 ? 2 * ws->backoff : 64;
-  }
-  if (ws->run > 0 && ws->ctrl_iters >= 0) {
-    const double pred = (double)ws->run_iters / ws->run, plain = 0.5 * (ws->ctrl_iters + res->iters);
-    if (pred > plain) {
-      ws->cooloff = ws->backoff;
-      ws->backoff = ws->backoff < 64 ? 2 * ws->backoff : 64;
-      ws->trust = 2;
+  if (warmstart == TL_WARM_EXTRAPOLATE && ws->nhist >= 1) {
+    double *ub = F.ub;
+    launch_halo(st, &ub, 1, g, 1, TL_MODE_TEALEAF);
+    CKL();
+    OpWarmResid op;
+    op.F = F;
+    op.g = g;
+    op.write = 1;
+    launch_walk<1>(st, op, ctx->walk_exact, g.ny);
+    CKL();
+    ctx->launches += 2;
+    if ((rc = tl_read_scalars(ctx))) return rc;
+    const double rr_pred = ctx->host_sc->red[0];
+    res->r0_pred = bb > 0 ? sqrt(rr_pred / bb) : sqrt(rr_pred);
+    if (rr_pred < rr_plain) {
+      if ((rc = accept_candidate(ctx))) return rc;
+      res->warm = 1;
     } else {
-      ws->trust = ws->trust < 32 ? 2 * ws->trust : 32;
-      ws->backoff = 4;
+      res->warm = 2;
     }
   }
-  ws->run = 0;
-  ws->run_iters = 0;
-  ws->ctrl_iters = res->iters;
+  // keep u^n as the newest earlier solution for the next step
+  double *oldest = ws->hist[2];
+  ws->hist[2] = ws->hist[1];
+  ws->hist[1] = ws->hist[0];
+  ws->hist[0] = oldest;
+  k_copy_u0<<<grid_cells(g), 256, 0, st>>>(F, g, ws->hist[0]);
+  CKL();
+  ctx->launches += 1;
+  ws->nhist = ws->nhist < 3 ? ws->nhist + 1 : 3;
+  return TL_OK;
 }

@@ -384,15 +384,18 @@ def train(trajs, steps: int, B: int = 16, size: int = 128, lr: float = 1e-4, see
 # A/B evaluation through the solver
 # ---------------------------------------------------------------------------
 
-MODES = {"plain": _abi.WARM_OFF, "network": _abi.WARM_NETWORK, "extrapolate": _abi.WARM_EXTRAPOLATE}
+MODES = {"plain": _abi.WARM_OFF, "network": _abi.WARM_NETWORK, "extrapolate": _abi.WARM_EXTRAPOLATE,
+         "history": _abi.WARM_HISTORY}
 
 
-def evaluate(tl, params, n: int, seed: int, steps: int, precision: int, modes=("plain", "network", "extrapolate"),
-             log=None):
-    """The same deck solved from the plain start, with the network's warm
-    start and with plain extrapolation (the network with g = 0): iterations,
-    device time and warm-start decision per step, and the final u of each
-    relative to the plain-start run."""
+def evaluate(tl, params, n: int, seed: int, steps: int, precision: int,
+             modes=("plain", "extrapolate", "history", "network"), log=None):
+    """The same deck solved from the plain start u^n, from the linear
+    extrapolation 2u^n - u^{n-1}, from the A-norm projection onto the history
+    (u^n and the last three increments) and from the projection with the
+    network's correction added: iterations, device time, warm-start decision
+    and weights per step, and the final u of each relative to the plain-start
+    run."""
     out, fields = {}, {}
     for name in modes:
         s = tl.Settings.from_text(deck_text(n, seed, steps), mode=_abi.MODE_TEALEAF, exact=False,
@@ -401,7 +404,7 @@ def evaluate(tl, params, n: int, seed: int, steps: int, precision: int, modes=("
         if MODES[name] == _abi.WARM_NETWORK:
             chunk.warm_load(params)
         rx, ry = s.dtinit / s.dx ** 2, s.dtinit / s.dy ** 2
-        iters, ms, used, r0p, r0q = [], [], [], [], []
+        iters, ms, used, r0p, r0q, coef = [], [], [], [], [], []
         for k in range(steps):
             chunk.check(chunk.lib.tl_synchronize(chunk.ctx))
             chunk.check(chunk.lib.tl_timer_start(chunk.ctx))
@@ -417,8 +420,9 @@ def evaluate(tl, params, n: int, seed: int, steps: int, precision: int, modes=("
             used.append(r.warm)
             r0p.append(r.r0_plain)
             r0q.append(r.r0_pred)
+            coef.append(list(r.warm_coef))
         hd = s.halodepth
-        out[name] = {"iters": iters, "ms": ms, "used": used, "r0_plain": r0p, "r0_pred": r0q}
+        out[name] = {"iters": iters, "ms": ms, "used": used, "r0_plain": r0p, "r0_pred": r0q, "coef": coef}
         fields[name] = chunk.field("u")[hd:-hd, hd:-hd].copy()
         chunk.close()
         if log:
