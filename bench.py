@@ -147,7 +147,7 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 
 # bench variants: (precision, warm start)
-# learned: the A-norm projection onto u^n, the last three increments and the
+# learned: the A-norm projection onto u^n, the last six increments and the
 # network's correction; history: the same projection without the network;
 # extrap: u^n + (u^n - u^{n-1})
 VARIANTS = {"learned_fp32_ir": (1, 1), "fp32_ir": (1, 0), "history_fp32_ir": (1, 3), "extrap_fp32_ir": (1, 2),
@@ -800,7 +800,7 @@ def run_config5(args):
             ev[pname] = {k: {"iters": sum(v["iters"]), "ms": sum(v["ms"]),
                              "predictions_used": sum(1 for u in v["used"] if u == 1),
                              "final_rel_diff": v.get("final_rel_diff"), "iters_per_step": v["iters"],
-                             "network_weight": [c[4] for c in v["coef"]]}
+                             "network_weight": [c[-1] for c in v["coef"]]}
                          for k, v in r.items()}
         line["eval"] = ev
         line["value"] = ev["fp32_ir"]["network"]["ms"] / args.steps

@@ -97,11 +97,12 @@ typedef struct {
                                contraction (bit-identical to the CPU restatement); 0: fused FMA kernels */
   int warmstart;            /* CG in tealeaf mode, the start when it beats the plain start u^n by
                                residual: 0 off; TL_WARM_NETWORK: the A-norm projection onto u^n, the
-                               last three increments and the warm-start network's correction
+                               last TL_WARM_HIST increments and the warm-start network's correction
                                (tl_warm_load); TL_WARM_HISTORY: the same projection without the
                                network; TL_WARM_EXTRAPOLATE: u^n + (u^n - u^{n-1}) */
 } tl_params;
 enum { TL_WARM_OFF = 0, TL_WARM_NETWORK = 1, TL_WARM_EXTRAPOLATE = 2, TL_WARM_HISTORY = 3 };
+#define TL_WARM_HIST 6      /* earlier right-hand sides the warm-start projection keeps */
 
 typedef struct {
   int iters;                /* trips of the solver's main loop                  */
@@ -120,8 +121,8 @@ typedef struct {
                                the smaller residual and was used */
   double r0_plain;          /* ||u0 - A u^n|| / ||u0|| of the plain start (warm start asked), else -1 */
   double r0_pred;           /* the same for the prediction, -1 when none was made */
-  double warm_coef[5];      /* the prediction's weights on u^n, u^{n-1}, u^{n-2}, u^{n-3} and on the
-                               network's correction g (u^n - u^{n-1}); zero when no prediction */
+  double warm_coef[TL_WARM_HIST + 2]; /* the prediction's weights on u^n, u^{n-1}, ..., u^{n-TL_WARM_HIST}
+                               and on the network's correction g (u^n - u^{n-1}); zero when none */
 } tl_result;
 
 /* Creation.  Replaces Chunk(set) (src/chunk.jl:68-89): allocates every field
@@ -275,7 +276,7 @@ int tl_parse_deck(const char *text, int mode, tl_deck *deck, tl_state *states, i
  * tensor cores) reads, per cell, u^n / rms(u^n), log(rx / density) / 4 and
  * (u^n - u^{n-1}) / rms(u^n - u^{n-1}) and returns a factor g; its prediction
  * of u^{n+1} is u^n + (1 + g) (u^n - u^{n-1}).  In the solve, the start is
- * the A-norm projection of the solution onto u^n, the last three increments
+ * the A-norm projection of the solution onto u^n, the last six increments
  * u^{n-k} - u^{n-k-1} and the network's correction g (u^n - u^{n-1}): the
  * combination closest to A^{-1} u^n in the A-norm, so never farther than the
  * plain start or the linear extrapolation.  The network's term is kept only

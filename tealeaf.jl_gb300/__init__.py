@@ -56,7 +56,7 @@ class SolveResult:
     warm: int = 0              # 0 plain start, 1 the prediction was used, 2 it lost to the plain start
     r0_plain: float = -1.0     # initial relative residual of the plain start (warm start asked)
     r0_pred: float = -1.0      # the same for the prediction (-1: none made)
-    warm_coef: tuple = ()      # the prediction's weights on u^n, u^{n-1}, u^{n-2}, u^{n-3}, network term
+    warm_coef: tuple = ()      # the prediction's weights on u^n, u^{n-1}, ..., u^{n-6}, network term
 
 
 class Chunk:

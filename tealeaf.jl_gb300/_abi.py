@@ -22,6 +22,7 @@ CRIT_REFERENCE, CRIT_RELATIVE = 0, 1
 PREC_FP64, PREC_FP32_IR = 0, 1
 GEOM_RECTANGULAR, GEOM_CIRCULAR, GEOM_POINT = 0, 1, 2
 WARM_OFF, WARM_NETWORK, WARM_EXTRAPOLATE, WARM_HISTORY = 0, 1, 2, 3
+WARM_HIST = 6          # TL_WARM_HIST: earlier right-hand sides of the warm-start projection
 
 
 class Config(C.Structure):
@@ -46,7 +47,7 @@ class Result(C.Structure):
     _fields_ = [("iters", C.c_int), ("cg_iters", C.c_int), ("inner_iters", C.c_int), ("est_iters", C.c_int),
                 ("error", C.c_double), ("eigmin", C.c_double), ("eigmax", C.c_double), ("converged", C.c_int),
                 ("refinements", C.c_int), ("rel_residual", C.c_double), ("launches", C.c_int), ("warm", C.c_int),
-                ("r0_plain", C.c_double), ("r0_pred", C.c_double), ("warm_coef", C.c_double * 5)]
+                ("r0_plain", C.c_double), ("r0_pred", C.c_double), ("warm_coef", C.c_double * (WARM_HIST + 2))]
 
 
 class Deck(C.Structure):

@@ -1,11 +1,11 @@
 // tl_warm.cu -- the warm start inside CG.solve! (tealeaf mode, FP64 and
 // FP32-refined CG).  After tea_leaf_init and copyu! the context holds
 // u = u0 = u^n and the plain start's residual r = p = u0 - A u^n.  The
-// context keeps the last three solutions u^{n-1}, u^{n-2}, u^{n-3}.
+// context keeps the last six right-hand sides u^{n-1}, ..., u^{n-6}.
 //
 // The candidate start is the A-norm projection of the solution u^{n+1} =
 // A^{-1} u0 onto a small basis: u^n, the increments u^n - u^{n-1},
-// u^{n-1} - u^{n-2}, u^{n-2} - u^{n-3} (those that exist), and, with the
+// u^{n-1} - u^{n-2}, ... (those that exist, up to six), and, with the
 // network, the network's correction g (u^n - u^{n-1}) (its prediction is
 // u^n + (1 + g)(u^n - u^{n-1})).  With V the basis, the start
 // x = V c minimises ||x - A^{-1} u0||_A over the span, from the Gram system
@@ -37,7 +37,8 @@ struct tl_warm_state {
   void *act = nullptr;                  // feature map (16 ch) + two 32-channel activation maps + g
   __nv_bfloat16 *feat = nullptr, *a0 = nullptr, *a1 = nullptr;
   float *g = nullptr;
-  double *hist[3] = {};                 // u^{n-1}, u^{n-2}, u^{n-3}, laid out like the context's fields
+  double *hist[TL_WARM_HIST] = {};      // u^{n-1}, u^{n-2}, ..., laid out like the context's fields
+  double *hist_base = nullptr;          // the one allocation they rotate through
   int nhist = 0;                        // how many of them hold an earlier step
   int net_skip = 0;                     // steps left before the network runs again
   int net_backoff = 1;                  // steps the next loss of the network's term skips (1, 2, ... 32)
@@ -88,83 +89,112 @@ __global__ void k_warm_stats_fold(double *part, int nblk) {
   part[2 * nblk + 1] = sd;
 }
 
-// The projection basis at one cell: v0 = u^n, then the increments
-// u^n - u^{n-1}, u^{n-1} - u^{n-2}, u^{n-2} - u^{n-3} (nh of them), then the
-// network's correction g (u^n - u^{n-1}) when `gv` is set.
-constexpr int PROJ_MAX = 5;
+// The projection basis.  Slot 0 holds u^n; slots 1..WARM_HIST the
+// increments u^n - u^{n-1}, u^{n-1} - u^{n-2}, ... (the first nh of them
+// exist, the others are zero); the last slot holds the network's correction
+// g (u^n - u^{n-1}) when the network ran, else zero.  Fixed slots keep every
+// index compile-time; the host solves the system on the slots in use.
+constexpr int WARM_HIST = TL_WARM_HIST;                  // earlier right-hand sides kept
+constexpr int PROJ_MAX = WARM_HIST + 2;                   // basis slots
+constexpr int PROJ_NET = PROJ_MAX - 1;                    // the network's slot
 constexpr int PROJ_NG = PROJ_MAX * (PROJ_MAX + 1) / 2;  // upper triangle of V^T A V
 constexpr int PROJ_NACC = PROJ_NG + PROJ_MAX;           // ... then V^T u0
 constexpr int GRAM_BLOCKS = 304;
 
 struct ProjBasis {
-  const double *u0, *h0, *h1, *h2;  // u^n, u^{n-1}, u^{n-2}, u^{n-3}
+  const double *u0;                 // u^n
+  const double *h[WARM_HIST];       // u^{n-1}, u^{n-2}, ... (the first nh are set)
   const float *gv;                  // network output g (interior, row-major), or null
-  int nh;                           // increments in the basis (1..3)
-  int m;                            // basis size: 1 + nh + (gv != null)
+  int nh;                           // increments in the basis (1..WARM_HIST)
 };
 
-__device__ __forceinline__ void basis_at(const ProjBasis &B, size_t c, long long k, double (&v)[PROJ_MAX]) {
-  const double u = B.u0[c], a = B.h0[c];
-  const double b = B.nh >= 2 ? B.h1[c] : 0.0, e = B.nh >= 3 ? B.h2[c] : 0.0;
-  const double net = B.gv ? (double)B.gv[k] * (u - a) : 0.0;
-  v[0] = u;
-  v[1] = u - a;
-  v[2] = B.nh >= 2 ? a - b : net;
-  v[3] = B.nh >= 3 ? b - e : (B.nh == 2 ? net : 0.0);
-  v[4] = B.nh >= 3 ? net : 0.0;
+// The right-hand sides u^n, u^{n-1}, ... at one cell (zero past nh).
+__device__ __forceinline__ void hist_at(const ProjBasis &B, size_t c, double (&hv)[WARM_HIST + 1]) {
+  hv[0] = B.u0[c];
+#pragma unroll
+  for (int i = 1; i <= WARM_HIST; ++i) hv[i] = i <= B.nh ? B.h[i - 1][c] : 0.0;
 }
 
-// One pass: A v_j at every interior cell for every basis vector (the
-// 5-point operator in difference form, v + sum k (v - v_nbr), with the
-// reflective boundary folded in: a neighbour across the edge is the cell
-// itself), and the sums v_a . A v_b (a <= b) and v_a . u0.  Fixed grid and
-// block order: the sums are deterministic.
+// The basis slots at one cell.
+__device__ __forceinline__ void basis_at(const ProjBasis &B, size_t c, long long k, double (&v)[PROJ_MAX]) {
+  double hv[WARM_HIST + 1];
+  hist_at(B, c, hv);
+  v[0] = hv[0];
+#pragma unroll
+  for (int j = 1; j <= WARM_HIST; ++j) v[j] = j <= B.nh ? hv[j - 1] - hv[j] : 0.0;
+  v[PROJ_NET] = B.gv ? (double)B.gv[k] * (hv[0] - hv[1]) : 0.0;
+}
+
+// The 5-point operator in difference form, v + sum k (v - v_nbr), with the
+// reflective boundary folded in (a neighbour across the edge is the cell).
+__device__ __forceinline__ double stencil(double vc, double ve, double vw, double vn, double vs, double kxE, double kxW,
+                                          double kyN, double kyS) {
+  return vc + kxE * (vc - ve) + kxW * (vc - vw) + kyN * (vc - vn) + kyS * (vc - vs);
+}
+
+// One pass: A v_j at every interior cell for every basis slot, from A of each
+// earlier right-hand side (an increment's A v is the difference of two), and
+// the sums v_a . A v_b (a <= b) and v_a . u0.  Fixed grid and block order:
+// the sums are deterministic.
 __global__ void __launch_bounds__(256) k_warm_gram(Fields F, Geom g, ProjBasis B, double *part) {
   double acc[PROJ_NACC];
 #pragma unroll
   for (int a = 0; a < PROJ_NACC; ++a) acc[a] = 0.0;
-  const int m = B.m;
   const long long n = (long long)g.nx * g.ny;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(k % g.nx), j = (int)(k / g.nx);
     const size_t c = g.at(i, j);
     const size_t cE = i + 1 < g.nx ? c + 1 : c, cW = i > 0 ? c - 1 : c;
     const size_t cN = j + 1 < g.ny ? c + g.pitch : c, cS = j > 0 ? c - g.pitch : c;
-    const long long kE = i + 1 < g.nx ? k + 1 : k, kW = i > 0 ? k - 1 : k;
-    const long long kN = j + 1 < g.ny ? k + g.nx : k, kS = j > 0 ? k - g.nx : k;
-    double vc[PROJ_MAX] = {}, vE[PROJ_MAX] = {}, vW[PROJ_MAX] = {}, vN[PROJ_MAX] = {}, vS[PROJ_MAX] = {};
-    basis_at(B, c, k, vc);
-    basis_at(B, cE, kE, vE);
-    basis_at(B, cW, kW, vW);
-    basis_at(B, cN, kN, vN);
-    basis_at(B, cS, kS, vS);
     const double kxE = F.kx[c + 1], kxW = F.kx[c], kyN = F.ky[c + g.pitch], kyS = F.ky[c];
-    double av[PROJ_MAX];
+    double hc[WARM_HIST + 1], ah[WARM_HIST + 1];
+    hist_at(B, c, hc);
+    ah[0] = stencil(hc[0], B.u0[cE], B.u0[cW], B.u0[cN], B.u0[cS], kxE, kxW, kyN, kyS);
 #pragma unroll
-    for (int b = 0; b < PROJ_MAX; ++b)
-      av[b] = vc[b] + kxE * (vc[b] - vE[b]) + kxW * (vc[b] - vW[b]) + kyN * (vc[b] - vN[b]) + kyS * (vc[b] - vS[b]);
-    int t = 0;
+    for (int q = 1; q <= WARM_HIST; ++q) {
+      ah[q] = 0.0;
+      if (q <= B.nh) {
+        const double *h = B.h[q - 1];
+        ah[q] = stencil(hc[q], h[cE], h[cW], h[cN], h[cS], kxE, kxW, kyN, kyS);
+      }
+    }
+    double v[PROJ_MAX], av[PROJ_MAX];
+    v[0] = hc[0];
+    av[0] = ah[0];
+#pragma unroll
+    for (int q = 1; q <= WARM_HIST; ++q) {
+      v[q] = q <= B.nh ? hc[q - 1] - hc[q] : 0.0;
+      av[q] = q <= B.nh ? ah[q - 1] - ah[q] : 0.0;
+    }
+    v[PROJ_NET] = av[PROJ_NET] = 0.0;
+    if (B.gv) {
+      const long long kE = i + 1 < g.nx ? k + 1 : k, kW = i > 0 ? k - 1 : k;
+      const long long kN = j + 1 < g.ny ? k + g.nx : k, kS = j > 0 ? k - g.nx : k;
+      const double *h0 = B.h[0];
+      auto t = [&](size_t cc, long long kk) { return (double)B.gv[kk] * (B.u0[cc] - h0[cc]); };
+      v[PROJ_NET] = (double)B.gv[k] * (hc[0] - hc[1]);
+      av[PROJ_NET] = stencil(v[PROJ_NET], t(cE, kE), t(cW, kW), t(cN, kN), t(cS, kS), kxE, kxW, kyN, kyS);
+    }
+    int tt = 0;
 #pragma unroll
     for (int a = 0; a < PROJ_MAX; ++a)
 #pragma unroll
-      for (int b = a; b < PROJ_MAX; ++b, ++t)
-        if (b < m) acc[t] = fma(vc[a], av[b], acc[t]);
+      for (int b = a; b < PROJ_MAX; ++b, ++tt) acc[tt] = fma(v[a], av[b], acc[tt]);
 #pragma unroll
-    for (int a = 0; a < PROJ_MAX; ++a)
-      if (a < m) acc[PROJ_NG + a] = fma(vc[a], vc[0], acc[PROJ_NG + a]);
+    for (int a = 0; a < PROJ_MAX; ++a) acc[PROJ_NG + a] = fma(v[a], v[0], acc[PROJ_NG + a]);
   }
   __shared__ double ws[8][PROJ_NACC];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int a = 0; a < PROJ_NACC; ++a) {
-    const double v = warp_butterfly(acc[a]);
-    if (lane == 0) ws[warp][a] = v;
+    const double val = warp_butterfly(acc[a]);
+    if (lane == 0) ws[warp][a] = val;
   }
   __syncthreads();
   if (threadIdx.x < PROJ_NACC) {
-    double v = ws[0][threadIdx.x];
-    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v += ws[w][threadIdx.x];
-    part[(size_t)blockIdx.x * PROJ_NACC + threadIdx.x] = v;
+    double val = ws[0][threadIdx.x];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) val += ws[w][threadIdx.x];
+    part[(size_t)blockIdx.x * PROJ_NACC + threadIdx.x] = val;
   }
 }
 
@@ -176,7 +206,7 @@ __global__ void k_warm_gram_fold(double *part, int nblk) {
 }
 
 struct ProjCoef {
-  double c[PROJ_MAX];
+  double c[PROJ_MAX];  // zero on the slots not in use
 };
 
 // x = V c on the interior, into ub.
@@ -184,12 +214,11 @@ __global__ void k_warm_combine(Fields F, Geom g, ProjBasis B, ProjCoef C) {
   const long long n = (long long)g.nx * g.ny;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
     const size_t c = g.at((int)(k % g.nx), (int)(k / g.nx));
-    double v[PROJ_MAX] = {};
+    double v[PROJ_MAX];
     basis_at(B, c, k, v);
     double x = 0.0;
 #pragma unroll
-    for (int a = 0; a < PROJ_MAX; ++a)
-      if (a < B.m) x = fma(C.c[a], v[a], x);
+    for (int a = 0; a < PROJ_MAX; ++a) x = fma(C.c[a], v[a], x);
     F.ub[c] = x;
   }
 }
@@ -265,7 +294,7 @@ void tl_release_warm(tl_ctx *ctx) {
   if (!ws) return;
   if (ws->wbuf) cudaFree(ws->wbuf);
   if (ws->act) cudaFree(ws->act);
-  if (ws->hist[0]) cudaFree(ws->hist[0]);  // one allocation holds the three
+  if (ws->hist_base) cudaFree(ws->hist_base);  // one allocation holds all of them (hist[] rotates)
   if (ws->stats) cudaFree(ws->stats);
   if (ws->crop) cudaFree(ws->crop);
   delete ws;
@@ -333,12 +362,13 @@ static int ensure_warm_buffers(tl_ctx *ctx, int network) {
   tl_warm_state *ws = ctx->warm;
   const Geom &g = ctx->g;
   const size_t cells = (size_t)g.nx * g.ny;
-  if (!ws->hist[0]) {
+  if (!ws->hist_base) {
     const size_t fb = sizeof(double) * (size_t)g.pitch * g.Y;
     double *h = nullptr;
-    CK(cudaMalloc(&h, 3 * fb));
-    CK(cudaMemsetAsync(h, 0, 3 * fb, ctx->stream));
-    for (int k = 0; k < 3; ++k) ws->hist[k] = h + (size_t)k * g.pitch * g.Y;
+    CK(cudaMalloc(&h, TL_WARM_HIST * fb));
+    CK(cudaMemsetAsync(h, 0, TL_WARM_HIST * fb, ctx->stream));
+    ws->hist_base = h;
+    for (int k = 0; k < TL_WARM_HIST; ++k) ws->hist[k] = h + (size_t)k * g.pitch * g.Y;
     CK(cudaMalloc(&ws->stats, sizeof(double) * (2 * STAT_BLOCKS + 2 + (size_t)(GRAM_BLOCKS + 1) * PROJ_NACC)));
     ws->gram = ws->stats + 2 * STAT_BLOCKS + 2;
     CK(cudaMalloc(&ws->crop, sizeof(tl_warm_crop)));
@@ -410,7 +440,23 @@ static int run_network(tl_ctx *ctx, double rx, double ry) {
 // diagonalised by cyclic Jacobi rotations, and directions whose eigenvalue is
 // below 1e-12 of the largest are dropped (nearly dependent increments).
 // Returns 0 when no usable solution exists.
-static int solve_gram(int m, const double *G, const double *h, double *c) {
+static int solve_dense(int m, const double *G, const double *h, double *c);
+
+// The same on the basis slots listed in `slot` (the rows and columns of the
+// full PROJ_MAX x PROJ_MAX system in use); c is zero on the other slots.
+static int solve_gram(int m, const int *slot, const double *G, const double *h, double *c) {
+  double Gl[PROJ_MAX * PROJ_MAX], hl[PROJ_MAX], cl[PROJ_MAX];
+  for (int a = 0; a < m; ++a) {
+    hl[a] = h[slot[a]];
+    for (int b = 0; b < m; ++b) Gl[a * PROJ_MAX + b] = G[slot[a] * PROJ_MAX + slot[b]];
+  }
+  for (int a = 0; a < PROJ_MAX; ++a) c[a] = 0.0;
+  if (!solve_dense(m, Gl, hl, cl)) return 0;
+  for (int a = 0; a < m; ++a) c[slot[a]] = cl[a];
+  return 1;
+}
+
+static int solve_dense(int m, const double *G, const double *h, double *c) {
   double S[PROJ_MAX][PROJ_MAX], Q[PROJ_MAX][PROJ_MAX], sc[PROJ_MAX], hs[PROJ_MAX];
   for (int a = 0; a < m; ++a) {
     if (!(G[a * PROJ_MAX + a] > 0) || !std::isfinite(G[a * PROJ_MAX + a])) return 0;
@@ -539,7 +585,7 @@ int tl_warm_try(tl_ctx *ctx, double rx, double ry, int warmstart, tl_result *res
   res->r0_plain = bb > 0 ? sqrt(rr_plain / bb) : sqrt(rr_plain);
   res->r0_pred = -1.0;
   res->warm = 0;
-  for (int a = 0; a < 5; ++a) res->warm_coef[a] = 0.0;
+  for (int a = 0; a < TL_WARM_HIST + 2; ++a) res->warm_coef[a] = 0.0;
   if (ws->nhist >= 1 && warmstart == TL_WARM_EXTRAPOLATE) {
     k_warm_extrapolate<<<grid_cells(g), 256, 0, st>>>(F, g, ws->hist[0]);
     CKL();
@@ -549,9 +595,7 @@ int tl_warm_try(tl_ctx *ctx, double rx, double ry, int warmstart, tl_result *res
   } else if (ws->nhist >= 1) {
     ProjBasis B;
     B.u0 = F.u0;
-    B.h0 = ws->hist[0];
-    B.h1 = ws->hist[1];
-    B.h2 = ws->hist[2];
+    for (int q = 0; q < TL_WARM_HIST; ++q) B.h[q] = ws->hist[q];
     B.nh = ws->nhist;
     B.gv = nullptr;
     if (network && ws->net_skip > 0) {
@@ -561,9 +605,8 @@ int tl_warm_try(tl_ctx *ctx, double rx, double ry, int warmstart, tl_result *res
       if (nrc < 0) return -nrc;
       if (nrc == 0) B.gv = ws->g;
     }
-    B.m = 1 + B.nh + (B.gv ? 1 : 0);
     k_warm_gram<<<GRAM_BLOCKS, 256, 0, st>>>(F, g, B, ws->gram);
-    k_warm_gram_fold<<<1, 32, 0, st>>>(ws->gram, GRAM_BLOCKS);
+    k_warm_gram_fold<<<1, 64, 0, st>>>(ws->gram, GRAM_BLOCKS);
     CKL();
     ctx->launches += 2;
     double tot[PROJ_NACC];
@@ -573,19 +616,20 @@ int tl_warm_try(tl_ctx *ctx, double rx, double ry, int warmstart, tl_result *res
     for (int a = 0, t = 0; a < PROJ_MAX; ++a)
       for (int b = a; b < PROJ_MAX; ++b, ++t) G[a * PROJ_MAX + b] = G[b * PROJ_MAX + a] = tot[t];
     for (int a = 0; a < PROJ_MAX; ++a) h[a] = tot[PROJ_NG + a];
-    // the history-only projection (the leading block of the system), and
-    // with the network the full one; the network's term is kept only when
-    // its candidate's residual is below the history-only candidate's
-    ProjCoef Ch{}, Cn{};
+    // the history-only projection (slots 0..nh), and with the network the
+    // full one; the network's term is kept only when its candidate's
+    // residual is below the history-only candidate's
+    int slot[PROJ_MAX];
     const int mh = 1 + B.nh;
-    const int okh = solve_gram(mh, G, h, Ch.c);
-    const int okn = B.gv ? solve_gram(B.m, G, h, Cn.c) : 0;
+    for (int q = 0; q < mh; ++q) slot[q] = q;
+    slot[mh] = PROJ_NET;
+    ProjCoef Ch{}, Cn{};
+    const int okh = solve_gram(mh, slot, G, h, Ch.c);
+    const int okn = B.gv ? solve_gram(mh + 1, slot, G, h, Cn.c) : 0;
     const ProjCoef *chosen = nullptr;
     if (okh && okn) {
-      ProjBasis Bh = B;
-      Bh.m = mh;
       double rr_h = 0.0, rr_n = 0.0;
-      if ((rc = candidate_residual(ctx, Bh, Ch, 0, &rr_h))) return rc;
+      if ((rc = candidate_residual(ctx, B, Ch, 0, &rr_h))) return rc;
       if ((rc = candidate_residual(ctx, B, Cn, 0, &rr_n))) return rc;
       if (rr_n < rr_h) {
         chosen = &Cn;
@@ -594,25 +638,22 @@ int tl_warm_try(tl_ctx *ctx, double rx, double ry, int warmstart, tl_result *res
       } else {
         // the network's term did not pay: skip the next 1, 2, 4, ... 32 inferences
         chosen = &Ch;
-        B.m = mh;
         res->warm = 3;
         ws->net_skip = ws->net_backoff;
         ws->net_backoff = ws->net_backoff < 32 ? 2 * ws->net_backoff : 32;
       }
     } else if (okh) {
       chosen = &Ch;
-      B.m = mh;
       res->warm = network ? 3 : 1;
     }
     if (chosen) {
       double rr_pred = 0.0;
       if ((rc = candidate_residual(ctx, B, *chosen, 1, &rr_pred))) return rc;
+      // weights on u^n, u^{n-1}, ...: x = c0 u^n + sum_j c_j (u^{n-j+1} - u^{n-j}) + c_net t
       const double *cc = chosen->c;
       res->warm_coef[0] = cc[0] + cc[1];
-      res->warm_coef[1] = (B.nh >= 2 ? cc[2] : 0.0) - cc[1];
-      res->warm_coef[2] = (B.nh >= 3 ? cc[3] : 0.0) - (B.nh >= 2 ? cc[2] : 0.0);
-      res->warm_coef[3] = B.nh >= 3 ? -cc[3] : 0.0;
-      res->warm_coef[4] = B.m > mh ? cc[mh] : 0.0;
+      for (int q = 1; q <= B.nh; ++q) res->warm_coef[q] = (q < B.nh ? cc[q + 1] : 0.0) - cc[q];
+      res->warm_coef[TL_WARM_HIST + 1] = cc[PROJ_NET];
       res->r0_pred = bb > 0 ? sqrt(rr_pred / bb) : sqrt(rr_pred);
       if (rr_pred < rr_plain) {
         if ((rc = accept_candidate(ctx))) return rc;
@@ -643,13 +684,12 @@ int tl_warm_try(tl_ctx *ctx, double rx, double ry, int warmstart, tl_result *res
     }
   }
   // keep u^n as the newest earlier solution for the next step
-  double *oldest = ws->hist[2];
-  ws->hist[2] = ws->hist[1];
-  ws->hist[1] = ws->hist[0];
+  double *oldest = ws->hist[TL_WARM_HIST - 1];
+  for (int q = TL_WARM_HIST - 1; q > 0; --q) ws->hist[q] = ws->hist[q - 1];
   ws->hist[0] = oldest;
   k_copy_u0<<<grid_cells(g), 256, 0, st>>>(F, g, ws->hist[0]);
   CKL();
   ctx->launches += 1;
-  ws->nhist = ws->nhist < 3 ? ws->nhist + 1 : 3;
+  ws->nhist = ws->nhist < TL_WARM_HIST ? ws->nhist + 1 : TL_WARM_HIST;
   return TL_OK;
 }

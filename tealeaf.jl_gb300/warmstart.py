@@ -392,7 +392,7 @@ def evaluate(tl, params, n: int, seed: int, steps: int, precision: int,
              modes=("plain", "extrapolate", "history", "network"), log=None):
     """The same deck solved from the plain start u^n, from the linear
     extrapolation 2u^n - u^{n-1}, from the A-norm projection onto the history
-    (u^n and the last three increments) and from the projection with the
+    (u^n and the last six increments) and from the projection with the
     network's correction added: iterations, device time, warm-start decision
     and weights per step, and the final u of each relative to the plain-start
     run."""

@@ -233,7 +233,7 @@ def _oracle_relative(text, steps=1):
         ch.halo(1, ["energy", "density"])
         res.append(ch.solve(s.dtinit / s.dx ** 2, s.dtinit / s.dy ** 2))
         ch.solve_finished()
-    return res, ch.field("u")
+    return res, ch.field("u").copy()    # a copy: the chunk's memory is freed with it
 
 
 FP32_U_RTOL = 1e-8            # two solutions that each meet 1e-10 relative (see test_gpu_oracle_relative.py)
