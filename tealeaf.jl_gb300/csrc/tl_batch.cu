@@ -392,12 +392,6 @@ __global__ void k_batch_refine_map(const DeckDesc *decks, BatchMap *map) {
   share(decks, map, act, map->total_w, map->first_r, map->nblk_r);
 }
 
-// The block totals the map shares out: the FP64 or the FP32 launches' grids.
-__global__ void k_batch_totals(BatchMap *map, int total_w, int total_u) {
-  map->total_w = total_w;
-  map->total_u = total_u;
-}
-
 // Rebuilds the block map over the decks still running and sets the loop
 // condition (any deck left).  A deck runs until `done` (FP64) or `finished`
 // (FP32 refinement, where `done` only ends an inner loop).
@@ -434,8 +428,7 @@ struct tl_batch {
   DeckDesc *d_decks = nullptr;
   BatchMap *d_map = nullptr;
   BatchMap *h_map = nullptr;
-  int total_w = 0, total_u = 0;        // blocks of the FP64 W and UR launches
-  int total_w32 = 0, total_u32 = 0;    // the same for the FP32 launches (their own occupancy)
+  int total_w = 0, total_u = 0;
   cudaGraphExec_t graph = nullptr;     // FP64 CG loop
   cudaGraphExec_t graph_ir = nullptr;  // FP32-refined CG loop
   int ir_ready = 0;                    // the deck table holds the FP32 buffers
@@ -462,8 +455,8 @@ int bfail(tl_batch *b, cudaError_t e, const char *what) {
 void launch_body(tl_batch *b, int ir, cudaGraphConditionalHandle h, int set_cond) {
   for (int parity = 0; parity < 2; ++parity) {
     if (ir) {
-      k_batch_ir_w<<<b->total_w32, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
-      k_batch_ir_ur<<<b->total_u32, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
+      k_batch_ir_w<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
+      k_batch_ir_ur<<<b->total_u, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
     } else {
       k_batch_w<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
       k_batch_ur<<<b->total_u, 256, 0, b->stream>>>(b->d_decks, b->d_map, parity);
@@ -471,9 +464,9 @@ void launch_body(tl_batch *b, int ir, cudaGraphConditionalHandle h, int set_cond
   }
   if (ir) {
     k_batch_refine_map<<<1, 256, 0, b->stream>>>(b->d_decks, b->d_map);
-    k_batch_ir_fold<<<b->total_w32, 256, 0, b->stream>>>(b->d_decks, b->d_map);
-    k_batch_ir_halo<<<b->total_w32, 256, 0, b->stream>>>(b->d_decks, b->d_map);
-    k_batch_ir_resid<<<b->total_w32, 256, 0, b->stream>>>(b->d_decks, b->d_map);
+    k_batch_ir_fold<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map);
+    k_batch_ir_halo<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map);
+    k_batch_ir_resid<<<b->total_w, 256, 0, b->stream>>>(b->d_decks, b->d_map);
   }
   k_batch_map<<<1, 256, 0, b->stream>>>(b->d_decks, b->d_map, h, set_cond, ir);
 }
@@ -584,17 +577,6 @@ extern "C" int tl_batch_create(tl_batch **out, tl_ctx *const *ctxs, int n) {
   if (b->total_u > maxb) b->total_u = maxb;
   if (b->total_w < n) b->total_w = n;
   if (b->total_u < n) b->total_u = n;
-  // the FP32 kernels hold more registers: launching the FP64 grids would
-  // run them in two waves
-  int occ_w32 = 0, occ_u32 = 0;
-  BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_w32, k_batch_ir_w, 256, 0));
-  BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_u32, k_batch_ir_ur, 256, 0));
-  b->total_w32 = (occ_w32 > 0 ? occ_w32 : 1) * sms;
-  b->total_u32 = (occ_u32 > 0 ? occ_u32 : 1) * sms;
-  if (b->total_w32 > maxb) b->total_w32 = maxb;
-  if (b->total_u32 > maxb) b->total_u32 = maxb;
-  if (b->total_w32 < n) b->total_w32 = n;
-  if (b->total_u32 < n) b->total_u32 = n;
   BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
   BCK(cudaEventCreate(&b->ev0));
   BCK(cudaEventCreate(&b->ev1));
@@ -713,7 +695,6 @@ int batch_solve_ir(tl_batch *b, const double *rx, const double *ry, const tl_par
     restore();
     return rc;
   }
-  k_batch_totals<<<1, 1, 0, b->stream>>>(b->d_map, b->total_w32, b->total_u32);
   k_batch_map<<<1, 256, 0, b->stream>>>(b->d_decks, b->d_map, 0, 0, 1);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess && !b->graph_ir) rc = build_graph(b, 1);
@@ -793,7 +774,6 @@ extern "C" int tl_batch_solve(tl_batch *b, const double *rx, const double *ry, c
     return rc;
   }
   if (prm->maxiters >= 1) {
-    k_batch_totals<<<1, 1, 0, b->stream>>>(b->d_map, b->total_w, b->total_u);
     k_batch_map<<<1, 256, 0, b->stream>>>(b->d_decks, b->d_map, 0, 0, 0);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess && !b->graph) rc = build_graph(b, 0);

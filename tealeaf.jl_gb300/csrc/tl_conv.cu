@@ -533,6 +533,306 @@ __global__ void __launch_bounds__(256) k_conv3x3_tc(ConvArgs a) {
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(2 * TCOLS));
 }
 
+
+// ---------------------------------------------------------------------------
+// Warp-specialised form: the same implicit GEMM, with the producer, the MMA
+// issuer and the epilogue decoupled by mbarriers instead of a block barrier
+// per row.
+// ---------------------------------------------------------------------------
+//
+// A persistent block walks tiles of 128 pixels x WS_ROWS rows (tile t,
+// t + grid, ...).  Ten warps:
+//   warp 0      producer: copies input rows (cp.async) into a ring of
+//               WS_RING staged rows, keeps WS_AHEAD rows in flight, and
+//               publishes a row on its `full` mbarrier once its copies have
+//               landed (each lane waits for its own copies, fences them for
+//               the tensor core's async proxy and arrives);
+//   warp 1      MMA issuer (one lane): waits for the three input rows of an
+//               output row and for a free accumulator, issues the 9 x CIN/16
+//               MMAs into one of WS_NACC tensor-memory accumulators, then
+//               commits the accumulator's `tfull` mbarrier and frees the
+//               input rows no later row needs (`empty`, by tcgen05.commit);
+//   warps 2..9  epilogue: wait for `tfull`, read the accumulator
+//               (tcgen05.ld; lane quadrant warp % 4, channel half
+//               (warp - 2) / 4), release it (`tempty`), then bias, GELU and
+//               the stores.
+// Rows stream across tile boundaries, so loads, MMAs and epilogues of
+// neighbouring rows and tiles overlap.  Every mbarrier wait is bounded: one
+// that runs out raises the block's abort flag (every role then leaves its
+// loop) and counts in g_conv_timeouts.
+constexpr int WS_RING = 8;    // staged input rows
+constexpr int WS_AHEAD = 4;   // rows in flight before the producer publishes one
+constexpr int WS_NACC = 4;    // tensor-memory accumulators (TCOLS columns each)
+constexpr int WS_ROWS = 16;   // output rows per tile
+constexpr int WS_THREADS = 320;
+static_assert(WS_RING >= WS_AHEAD + 3, "the ring must hold the rows in flight and the three rows of an MMA");
+
+template <int CIN, int COUT>
+struct SmemWS {
+  static constexpr int NC = CIN / 8;
+  static constexpr int ROWB = (FTP + 2) * 16;
+  static constexpr int SLOT = NC * ROWB;
+  static constexpr int KC = 9 * CIN / 8;
+  static constexpr int WB = KC * COUT * 16;
+  static constexpr int BIAS = WB + WS_RING * SLOT;
+  static constexpr int BAR = BIAS + 4 * COUT;                     // 8-byte aligned (SLOT, WB multiples of 16)
+  static constexpr int NBAR = 2 * WS_RING + 2 * WS_NACC + 1;       // full, empty, tfull, tempty, drain
+  static constexpr int MISC = BAR + 8 * NBAR;                      // tensor-memory address, abort flag
+  static constexpr int BYTES = MISC + 16;
+};
+
+__device__ __forceinline__ void bar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(saddr(bar)) : "memory");
+}
+
+// Bounded wait for the completion of `parity`; false (and the abort flag
+// raised) when it runs out or another role has aborted.
+__device__ __forceinline__ bool ws_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag) {
+  for (int it = 0; it < SPIN_LIMIT; ++it) {
+    if (bar_try(bar, parity)) return true;
+    if ((it & 1023) == 1023 && *abort_flag) return false;
+  }
+  if (atomicExch(const_cast<int *>(abort_flag), 1) == 0) atomicAdd(&g_conv_timeouts, 1);
+  return false;
+}
+
+struct WsTile {
+  int img, x0, y0, rows;
+};
+
+__device__ __forceinline__ WsTile ws_tile(int t, int tiles_x, int tiles_y, int H) {
+  WsTile r;
+  r.img = t / (tiles_x * tiles_y);
+  const int rem = t % (tiles_x * tiles_y);
+  r.x0 = (rem % tiles_x) * FTP;
+  r.y0 = (rem / tiles_x) * WS_ROWS;
+  r.rows = min(WS_ROWS, H - r.y0);
+  return r;
+}
+
+template <int CIN, int COUT, int MODE>
+__global__ void __launch_bounds__(WS_THREADS) k_conv3x3_ws(ConvArgs a, int tiles_x, int tiles_y) {
+  using S = SmemWS<CIN, COUT>;
+  static_assert(COUT % 16 == 0 && COUT <= TCOLS && CIN % 16 == 0, "tile shape");
+  constexpr uint32_t ID = idesc(128, COUT);
+  constexpr int CH = COUT / 2;
+  extern __shared__ __align__(128) unsigned char smem[];
+  unsigned char *sw = smem;
+  unsigned char *sx = smem + S::WB;
+  float *sbias = reinterpret_cast<float *>(smem + S::BIAS);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + S::BAR);
+  uint64_t *full = bars, *empty = bars + WS_RING, *tfull = bars + 2 * WS_RING, *tempty = tfull + WS_NACC;
+  uint64_t *drain = tempty + WS_NACC;
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + S::MISC);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + S::MISC + 4);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int ntiles = a.N * tiles_x * tiles_y;
+  const size_t plane = (size_t)a.H * a.W;
+
+  if (tid == 0) {
+    for (int k = 0; k < WS_RING; ++k) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 32;\n" ::"r"(saddr(full + k)));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(empty + k)));
+    }
+    for (int k = 0; k < WS_NACC; ++k) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(tfull + k)));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 256;\n" ::"r"(saddr(tempty + k)));
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(drain)));
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    *abort_flag = 0;
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr(tslot)),
+                 "r"(WS_NACC * TCOLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+  }
+  if (tid < COUT) sbias[tid] = a.bias ? a.bias[tid] : 0.f;
+  for (int v = tid; v < COUT * S::KC; v += WS_THREADS) {
+    const int co = v / S::KC, kc = v % S::KC;
+    cp_async16(sw + (kc * COUT + co) * 16, a.w + (size_t)co * 9 * CIN + kc * 8, 16);
+  }
+  cp_async_wait_all();
+  fence_async_smem();
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = *tslot;
+  const uint32_t wbase = saddr(sw), xbase = saddr(sx);
+
+  if (warp == 0) {
+    // ---- producer ----
+    uint32_t L = 0, pub = 0;  // rows issued, rows published
+    bool ok = true;
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      const WsTile T = ws_tile(t, tiles_x, tiles_y, a.H);
+      const bf16 *xi = a.x + (size_t)T.img * plane * CIN;
+      for (int r = 0; r < T.rows + 2 && ok; ++r, ++L) {
+        const int slot = L % WS_RING;
+        const uint32_t use = L / WS_RING;
+        if (use > 0 && !ws_wait(empty + slot, (use - 1) & 1u, abort_flag)) {
+          ok = false;
+          break;
+        }
+        const int yy = T.y0 - 1 + r;
+        unsigned char *dst = sx + slot * S::SLOT;
+        for (int v = lane; v < (FTP + 2) * S::NC; v += 32) {
+          const int col = v / S::NC, c8 = v % S::NC, xx = T.x0 + col - 1;
+          const bool in = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
+          const bf16 *src = in ? xi + ((size_t)yy * a.W + xx) * CIN + c8 * 8 : xi;
+          cp_async16(dst + c8 * S::ROWB + col * 16, src, in ? 16 : 0);
+        }
+        cp_async_commit();
+        if (L + 1 - pub > (uint32_t)WS_AHEAD) {  // publish the oldest row in flight
+          asm volatile("cp.async.wait_group %0;\n" ::"n"(WS_AHEAD) : "memory");
+          fence_async_smem();
+          bar_arrive(full + pub % WS_RING);
+          ++pub;
+        }
+      }
+    }
+    cp_async_wait_all();
+    fence_async_smem();
+    for (; pub < L; ++pub) bar_arrive(full + pub % WS_RING);
+  } else if (warp == 1) {
+    // ---- MMA issuer ----
+    if (lane == 0) {
+      uint32_t L = 0, seen = 0, O = 0;  // rows of the tiles so far, rows waited for, output rows
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        const WsTile T = ws_tile(t, tiles_x, tiles_y, a.H);
+        const uint32_t base = L;
+        for (int i = 0; i < T.rows; ++i, ++O) {
+          for (; seen <= base + i + 2; ++seen)
+            if (!ws_wait(full + seen % WS_RING, (seen / WS_RING) & 1u, abort_flag)) {
+              ok = false;
+              break;
+            }
+          const int acc = O % WS_NACC;
+          const uint32_t use = O / WS_NACC;
+          if (ok && use > 0 && !ws_wait(tempty + acc, (use - 1) & 1u, abort_flag)) ok = false;
+          if (!ok) break;
+          fence_after();
+          const uint32_t d = tmem + acc * TCOLS;
+#pragma unroll
+          for (int dy = 0; dy < 3; ++dy) {
+            const uint32_t rbase = xbase + ((base + i + dy) % WS_RING) * S::SLOT;
+#pragma unroll
+            for (int dx = 0; dx < 3; ++dx) {
+              const int tap = 3 * dy + dx;
+#pragma unroll
+              for (int cc = 0; cc < CIN; cc += 16) {
+                const uint64_t ad = sdesc(rbase + (cc / 8) * S::ROWB + dx * 16, S::ROWB, 128);
+                const uint64_t bd = sdesc(wbase + ((tap * CIN + cc) / 8) * COUT * 16, COUT * 16, 128);
+                mma(d, ad, bd, ID, (tap | cc) != 0);
+              }
+            }
+          }
+          commit(tfull + acc);
+          // input row base + i is needed by no later output row of this tile;
+          // after the tile's last row its two bottom rows are free as well
+          commit(empty + (base + i) % WS_RING);
+          if (i == T.rows - 1) {
+            commit(empty + (base + i + 1) % WS_RING);
+            commit(empty + (base + i + 2) % WS_RING);
+          }
+        }
+        L += T.rows + 2;
+      }
+      // every MMA issued has completed before the block leaves (bounded, and
+      // waited for even after an abort: tensor memory is freed below)
+      commit(drain);
+      bool drained = false;
+      for (int it = 0; it < SPIN_LIMIT && !drained; ++it) drained = bar_try(drain, 0u);
+      if (!drained) atomicAdd(&g_conv_timeouts, 1);
+    }
+    __syncwarp();
+  } else {
+    // ---- epilogue ----
+    const int ew = warp - 2, quad = warp & 3, half = ew >> 2;
+    uint32_t O = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      const WsTile T = ws_tile(t, tiles_x, tiles_y, a.H);
+      const int xx = T.x0 + 32 * quad + lane;
+      for (int i = 0; i < T.rows; ++i, ++O) {
+        const int y = T.y0 + i;
+        uint4 gzv[MODE == 2 ? CH / 8 : 1];
+        if (MODE == 2 && xx < a.W) {
+          const uint4 *gp = reinterpret_cast<const uint4 *>(
+              a.gz + ((size_t)T.img * plane + (size_t)y * a.W + xx) * COUT + half * CH);
+#pragma unroll
+          for (int q = 0; q < (MODE == 2 ? CH / 8 : 1); ++q) gzv[q] = gp[q];
+        }
+        const int acc_i = O % WS_NACC;
+        if (!ws_wait(tfull + acc_i, (O / WS_NACC) & 1u, abort_flag)) {
+          ok = false;
+          break;
+        }
+        fence_after();
+        float acc[CH];
+        {
+          const uint32_t ta = tmem + ((uint32_t)(32 * quad) << 16) + acc_i * TCOLS + half * CH;
+          if (CH == 16) {
+            float v[16];
+            tld16(ta, v);
+#pragma unroll
+            for (int k = 0; k < CH; ++k) acc[k] = v[k];
+          } else {
+            float v[8];
+            tld8(ta, v);
+#pragma unroll
+            for (int k = 0; k < CH; ++k) acc[k] = v[k];
+          }
+        }
+        fence_before();
+        bar_arrive(tempty + acc_i);
+        if (xx < a.W) {
+          const size_t pix = (size_t)T.img * plane + (size_t)y * a.W + xx;
+#pragma unroll
+          for (int c = 0; c < CH; ++c) acc[c] += sbias[half * CH + c];
+          if (a.out32 && half == 0) a.out32[pix] = acc[0];
+          uint4 zo[CH / 8], oo[CH / 8];
+#pragma unroll
+          for (int q = 0; q < CH / 8; ++q) {
+            __nv_bfloat162 *zp = reinterpret_cast<__nv_bfloat162 *>(&zo[q]);
+            __nv_bfloat162 *op = reinterpret_cast<__nv_bfloat162 *>(&oo[q]);
+            const __nv_bfloat162 *gq = reinterpret_cast<const __nv_bfloat162 *>(&gzv[MODE == 2 ? q : 0]);
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+              const float z0 = acc[8 * q + 2 * h], z1 = acc[8 * q + 2 * h + 1];
+              float o0 = z0, o1 = z1;
+              if (MODE == 1) {
+                zp[h] = __floats2bfloat162_rn(z0, z1);
+                o0 = gelu_hw(z0);
+                o1 = gelu_hw(z1);
+              } else if (MODE == 2) {
+                o0 = z0 * gelu_grad_hw(__low2float(gq[h]));
+                o1 = z1 * gelu_grad_hw(__high2float(gq[h]));
+              }
+              op[h] = __floats2bfloat162_rn(o0, o1);
+            }
+          }
+          if (MODE == 1 && a.z) {
+            uint4 *zd = reinterpret_cast<uint4 *>(a.z + pix * COUT + half * CH);
+#pragma unroll
+            for (int q = 0; q < CH / 8; ++q) zd[q] = zo[q];
+          }
+          if (a.out) {
+            uint4 *od = reinterpret_cast<uint4 *>(a.out + pix * COUT + half * CH);
+#pragma unroll
+            for (int q = 0; q < CH / 8; ++q) od[q] = oo[q];
+          }
+        }
+      }
+    }
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(WS_NACC * TCOLS));
+}
+
 }  // namespace tc
 
 // Weight and bias gradients: dW[co][tap][ci] = sum_p dz[p][co] x[p + off(tap)][ci]
@@ -795,14 +1095,29 @@ inline int grid_for(long long n) {
   return (int)(b < 1 ? 1 : b);
 }
 
-// The forward kernel: tcgen05 by default; TEALEAF_GB300_CONV=mma selects the
-// warp-level mma.sync kernel (kept for comparison).
-bool conv_use_mma() {
+// The forward kernel: the warp-specialised tcgen05 kernel by default;
+// TEALEAF_GB300_CONV=tc selects the row-synchronous tcgen05 kernel and
+// TEALEAF_GB300_CONV=mma the warp-level mma.sync one (both kept for comparison).
+int conv_kind() {
   static const int v = [] {
     const char *e = getenv("TEALEAF_GB300_CONV");
-    return (e && !strcmp(e, "mma")) ? 1 : 0;
+    if (e && !strcmp(e, "mma")) return 2;
+    if (e && !strcmp(e, "tc")) return 1;
+    return 0;
   }();
-  return v != 0;
+  return v;
+}
+bool conv_use_mma() { return conv_kind() == 2; }
+
+int conv_sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        n < 1)
+      n = 152;
+  }
+  return n;
 }
 
 template <int CIN, int COUT, int MODE>
@@ -818,13 +1133,26 @@ void launch_conv_mode(const ConvArgs &a, cudaStream_t st) {
     k_conv3x3<CIN, COUT, MODE><<<grid, 128, smem, st>>>(a);
     return;
   }
-  constexpr int smem = tc::Smem<CIN, COUT>::BYTES;
+  if (conv_kind() == 1) {
+    constexpr int smem = tc::Smem<CIN, COUT>::BYTES;
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(tc::k_conv3x3_tc<CIN, COUT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+      attr = true;
+    }
+    tc::k_conv3x3_tc<CIN, COUT, MODE><<<grid, 256, smem, st>>>(a);
+    return;
+  }
+  constexpr int smem = tc::SmemWS<CIN, COUT>::BYTES;
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(tc::k_conv3x3_tc<CIN, COUT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(tc::k_conv3x3_ws<CIN, COUT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     attr = true;
   }
-  tc::k_conv3x3_tc<CIN, COUT, MODE><<<grid, 256, smem, st>>>(a);
+  const int tiles_x = (a.W + FTP - 1) / FTP, tiles_y = (a.H + tc::WS_ROWS - 1) / tc::WS_ROWS;
+  const long long tiles = (long long)a.N * tiles_x * tiles_y;
+  const long long blocks = tiles < 2LL * conv_sm_count() ? tiles : 2LL * conv_sm_count();
+  tc::k_conv3x3_ws<CIN, COUT, MODE><<<(int)blocks, tc::WS_THREADS, smem, st>>>(a, tiles_x, tiles_y);
 }
 
 template <int CIN, int COUT>
@@ -841,6 +1169,7 @@ int tl_conv_forward(const void *x, const void *w, const float *bias, const void 
   if (!x || !w || (!out && !out32) || N < 1 || H < 1 || W < 1 || mode < 0 || mode > 2) return TL_ERR_ARG;
   if (mode == 2 && !gz) return TL_ERR_ARG;
   if (N > 65535 || (H + FRB - 1) / FRB > 65535) return TL_ERR_ARG;
+  if ((long long)N * ((W + FTP - 1) / FTP) * ((H + tc::WS_ROWS - 1) / tc::WS_ROWS) > 2147483647LL) return TL_ERR_ARG;
   ConvArgs a;
   a.x = static_cast<const bf16 *>(x);
   a.w = static_cast<const bf16 *>(w);

