@@ -34,6 +34,7 @@ namespace {
 constexpr int BATCH_MAX = 1024;  // decks per batch
 constexpr int BATCH_WARPS = 8;
 constexpr int BATCH_ROWS = 8;
+constexpr int BATCH_ROWS32 = 32;  // rows of an FP32 warp tile: longer walks hide the row prefetch's latency
 
 // Work is handed out per warp: a warp tile is one warp's column strip (64
 // columns for the FP64 kernels, 128 for the FP32 ones) over BATCH_ROWS rows,
@@ -182,8 +183,8 @@ __device__ __forceinline__ void walk_deck32(const DeckDesc &D, const Op &op, int
   for (int t = lb * nw + warp; t < D.tiles32; t += nblocks * nw) {
     const int tx = t % D.ntx32, ty = t / D.ntx32;
     const int i0 = tx * 128 + 4 * lane;
-    const int j0 = ty * BATCH_ROWS;
-    const int j1 = min(j0 + BATCH_ROWS, D.g.ny);
+    const int j0 = ty * BATCH_ROWS32;
+    const int j1 = min(j0 + BATCH_ROWS32, D.g.ny);
     op.tile(i0, j0, j1, acc);
   }
 }
@@ -654,7 +655,7 @@ int batch_solve_ir(tl_batch *b, const double *rx, const double *ry, const tl_par
       D.p32 = ctx->ir->p;
       D.pb32 = ctx->ir->pb;
       D.ntx32 = (ctx->g.nx + 127) / 128;
-      D.tiles32 = D.ntx32 * ((ctx->g.ny + BATCH_ROWS - 1) / BATCH_ROWS);
+      D.tiles32 = D.ntx32 * ((ctx->g.ny + BATCH_ROWS32 - 1) / BATCH_ROWS32);
     }
     BCK(cudaMemcpyAsync(b->d_decks, b->h_decks.data(), sizeof(DeckDesc) * n, cudaMemcpyHostToDevice, b->stream));
     BCK(cudaStreamSynchronize(b->stream));

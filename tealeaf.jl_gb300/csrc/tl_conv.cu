@@ -560,14 +560,26 @@ __global__ void __launch_bounds__(256) k_conv3x3_tc(ConvArgs a) {
 // neighbouring rows and tiles overlap.  Every mbarrier wait is bounded: one
 // that runs out raises the block's abort flag (every role then leaves its
 // loop) and counts in g_conv_timeouts.
-constexpr int WS_RING = 8;    // staged input rows
-constexpr int WS_AHEAD = 4;   // rows in flight before the producer publishes one
 constexpr int WS_NACC = 4;    // tensor-memory accumulators (TCOLS columns each)
 constexpr int WS_ROWS = 16;   // output rows per tile
-constexpr int WS_THREADS = 320;
-static_assert(WS_RING >= WS_AHEAD + 3, "the ring must hold the rows in flight and the three rows of an MMA");
 
-template <int CIN, int COUT>
+// Pipeline shapes: RING staged rows, AHEAD rows in flight before the
+// producer publishes one, NPROD producer warps (10 + NPROD - 1 warps).
+// RS: row streaming.  Each staged input row is read by the tensor core
+// once per (dx, 16-channel step), with N = up to three output rows' channels
+// (the weights of dy = 2, 1, 0 stacked), accumulating into the three output
+// rows it feeds; otherwise each output row reads its three input rows.
+template <int RING_, int AHEAD_, int NPROD_, bool RS_ = false, int NACC_ = (RS_ ? 8 : WS_NACC)>
+struct WsCfg {
+  static constexpr int RING = RING_, AHEAD = AHEAD_, NPROD = NPROD_;
+  static constexpr bool RS = RS_;
+  static constexpr int NACC = NACC_;             // accumulator slots
+  static_assert(!RS || NACC >= 4, "a row-streaming window holds three slots while one is read");
+  static constexpr int THREADS = 32 * (NPROD + 9);
+  static_assert(RING >= AHEAD + 3, "the ring must hold the rows in flight and the three rows of an MMA");
+};
+
+template <int CIN, int COUT, int WS_RING, int NACC = WS_NACC>
 struct SmemWS {
   static constexpr int NC = CIN / 8;
   static constexpr int ROWB = (FTP + 2) * 16;
@@ -576,7 +588,7 @@ struct SmemWS {
   static constexpr int WB = KC * COUT * 16;
   static constexpr int BIAS = WB + WS_RING * SLOT;
   static constexpr int BAR = BIAS + 4 * COUT;                     // 8-byte aligned (SLOT, WB multiples of 16)
-  static constexpr int NBAR = 2 * WS_RING + 2 * WS_NACC + 1;       // full, empty, tfull, tempty, drain
+  static constexpr int NBAR = 2 * WS_RING + 2 * NACC + 1;          // full, empty, tfull, tempty, drain
   static constexpr int MISC = BAR + 8 * NBAR;                      // tensor-memory address, abort flag
   static constexpr int BYTES = MISC + 16;
 };
@@ -610,9 +622,15 @@ __device__ __forceinline__ WsTile ws_tile(int t, int tiles_x, int tiles_y, int H
   return r;
 }
 
-template <int CIN, int COUT, int MODE>
-__global__ void __launch_bounds__(WS_THREADS) k_conv3x3_ws(ConvArgs a, int tiles_x, int tiles_y) {
-  using S = SmemWS<CIN, COUT>;
+template <int CIN, int COUT, int MODE, class CFG>
+__global__ void __launch_bounds__(CFG::THREADS) k_conv3x3_ws(ConvArgs a, int tiles_x, int tiles_y) {
+  constexpr int WS_RING = CFG::RING, WS_AHEAD = CFG::AHEAD, NPROD = CFG::NPROD, WS_THREADS = CFG::THREADS;
+  constexpr int MMA_WARP = NPROD, EPI0 = NPROD + 1;
+  constexpr bool RS = CFG::RS;
+  constexpr int NACC = CFG::NACC;
+  constexpr int SW = RS ? COUT : TCOLS;                           // tensor-memory columns per accumulator slot
+  constexpr int TALLOC = NACC * SW <= 32 ? 32 : (NACC * SW <= 64 ? 64 : (NACC * SW <= 128 ? 128 : 256));
+  using S = SmemWS<CIN, COUT, WS_RING, NACC>;
   static_assert(COUT % 16 == 0 && COUT <= TCOLS && CIN % 16 == 0, "tile shape");
   constexpr uint32_t ID = idesc(128, COUT);
   constexpr int CH = COUT / 2;
@@ -621,8 +639,8 @@ __global__ void __launch_bounds__(WS_THREADS) k_conv3x3_ws(ConvArgs a, int tiles
   unsigned char *sx = smem + S::WB;
   float *sbias = reinterpret_cast<float *>(smem + S::BIAS);
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + S::BAR);
-  uint64_t *full = bars, *empty = bars + WS_RING, *tfull = bars + 2 * WS_RING, *tempty = tfull + WS_NACC;
-  uint64_t *drain = tempty + WS_NACC;
+  uint64_t *full = bars, *empty = bars + WS_RING, *tfull = bars + 2 * WS_RING, *tempty = tfull + NACC;
+  uint64_t *drain = tempty + NACC;
   uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + S::MISC);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + S::MISC + 4);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -631,10 +649,10 @@ __global__ void __launch_bounds__(WS_THREADS) k_conv3x3_ws(ConvArgs a, int tiles
 
   if (tid == 0) {
     for (int k = 0; k < WS_RING; ++k) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 32;\n" ::"r"(saddr(full + k)));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(saddr(full + k)), "r"(32 * NPROD));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(empty + k)));
     }
-    for (int k = 0; k < WS_NACC; ++k) {
+    for (int k = 0; k < NACC; ++k) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(tfull + k)));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 256;\n" ::"r"(saddr(tempty + k)));
     }
@@ -642,15 +660,26 @@ __global__ void __launch_bounds__(WS_THREADS) k_conv3x3_ws(ConvArgs a, int tiles
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     *abort_flag = 0;
   }
-  if (warp == 1) {
+  if (warp == MMA_WARP) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr(tslot)),
-                 "r"(WS_NACC * TCOLS));
+                 "r"(TALLOC));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
   }
   if (tid < COUT) sbias[tid] = a.bias ? a.bias[tid] : 0.f;
-  for (int v = tid; v < COUT * S::KC; v += WS_THREADS) {
-    const int co = v / S::KC, kc = v % S::KC;
-    cp_async16(sw + (kc * COUT + co) * 16, a.w + (size_t)co * 9 * CIN + kc * 8, 16);
+  if constexpr (RS) {
+    // [dx][k chunk][dy = 2, 1, 0][COUT][8 k values]: the B operand of an
+    // input row's (dx, channel step) MMA, up to three output rows stacked
+    for (int v = tid; v < 9 * S::NC * COUT; v += WS_THREADS) {
+      const int co = v % COUT, d = (v / COUT) % 3, kc = (v / (3 * COUT)) % S::NC, dx = v / (3 * COUT * S::NC);
+      const int tap = 3 * (2 - d) + dx;
+      cp_async16(sw + (((dx * S::NC + kc) * 3 + d) * COUT + co) * 16, a.w + (size_t)co * 9 * CIN + tap * CIN + kc * 8,
+                 16);
+    }
+  } else {
+    for (int v = tid; v < COUT * S::KC; v += WS_THREADS) {
+      const int co = v / S::KC, kc = v % S::KC;
+      cp_async16(sw + (kc * COUT + co) * 16, a.w + (size_t)co * 9 * CIN + kc * 8, 16);
+    }
   }
   cp_async_wait_all();
   fence_async_smem();
@@ -660,8 +689,8 @@ __global__ void __launch_bounds__(WS_THREADS) k_conv3x3_ws(ConvArgs a, int tiles
   const uint32_t tmem = *tslot;
   const uint32_t wbase = saddr(sw), xbase = saddr(sx);
 
-  if (warp == 0) {
-    // ---- producer ----
+  if (warp < NPROD) {
+    // ---- producers: warp w copies pixels-chunks w*32 + lane, step 32 * NPROD ----
     uint32_t L = 0, pub = 0;  // rows issued, rows published
     bool ok = true;
     for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
@@ -676,7 +705,7 @@ __global__ void __launch_bounds__(WS_THREADS) k_conv3x3_ws(ConvArgs a, int tiles
         }
         const int yy = T.y0 - 1 + r;
         unsigned char *dst = sx + slot * S::SLOT;
-        for (int v = lane; v < (FTP + 2) * S::NC; v += 32) {
+        for (int v = lane + 32 * warp; v < (FTP + 2) * S::NC; v += 32 * NPROD) {
           const int col = v / S::NC, c8 = v % S::NC, xx = T.x0 + col - 1;
           const bool in = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
           const bf16 *src = in ? xi + ((size_t)yy * a.W + xx) * CIN + c8 * 8 : xi;
@@ -694,9 +723,68 @@ __global__ void __launch_bounds__(WS_THREADS) k_conv3x3_ws(ConvArgs a, int tiles
     cp_async_wait_all();
     fence_async_smem();
     for (; pub < L; ++pub) bar_arrive(full + pub % WS_RING);
-  } else if (warp == 1) {
+  } else if (warp == MMA_WARP) {
     // ---- MMA issuer ----
-    if (lane == 0) {
+    if (RS && lane == 0) {
+      // one pass per staged input row t of a tile (image row y0 - 1 + t): it
+      // feeds output rows t - 2 (dy = 2), t - 1 (dy = 1) and t (dy = 0) of the
+      // tile, whose accumulators sit in consecutive slots; out(t) starts here
+      // (its first MMA does not accumulate) and out(t - 2) is complete after
+      uint32_t L = 0, O = 0;  // input rows and output rows of the tiles so far
+      bool ok = true;
+      auto run = [&](uint32_t Ob, int t, int oa, int ob, uint64_t ad, uint32_t bchunk, uint32_t acc) {
+        // outputs oa..ob (consecutive slots, split where the slot ring wraps)
+        const int sa = (int)((Ob + oa) % NACC);
+        const int cnt = ob - oa + 1, c1 = sa + cnt <= NACC ? cnt : NACC - sa;
+        const int d0 = oa - (t - 2);  // B block of output oa: dy = 2 - d0
+        mma(tmem + sa * SW, ad, sdesc(bchunk + d0 * COUT * 16, 3 * COUT * 16, 128), idesc(128, c1 * COUT), acc);
+        if (c1 < cnt)
+          mma(tmem, ad, sdesc(bchunk + (d0 + c1) * COUT * 16, 3 * COUT * 16, 128), idesc(128, (cnt - c1) * COUT), acc);
+      };
+      for (int tt = blockIdx.x; tt < ntiles && ok; tt += gridDim.x) {
+        const WsTile T = ws_tile(tt, tiles_x, tiles_y, a.H);
+        for (int t = 0; t < T.rows + 2; ++t) {
+          const uint32_t Lt = L + t;
+          if (!ws_wait(full + Lt % WS_RING, (Lt / WS_RING) & 1u, abort_flag)) {
+            ok = false;
+            break;
+          }
+          const int o1 = t - 2 > 0 ? t - 2 : 0, o2 = t < T.rows - 1 ? t : T.rows - 1;
+          const bool fresh = t <= T.rows - 1;
+          if (fresh) {
+            const uint32_t Og = O + t, use = Og / NACC;
+            if (use > 0 && !ws_wait(tempty + Og % NACC, (use - 1) & 1u, abort_flag)) {
+              ok = false;
+              break;
+            }
+          }
+          fence_after();
+          const uint32_t rbase = xbase + (Lt % WS_RING) * S::SLOT;
+#pragma unroll
+          for (int dx = 0; dx < 3; ++dx) {
+#pragma unroll
+            for (int cc = 0; cc < CIN; cc += 16) {
+              const uint64_t ad = sdesc(rbase + (cc / 8) * S::ROWB + dx * 16, S::ROWB, 128);
+              const uint32_t bchunk = wbase + (dx * S::NC + cc / 8) * 3 * COUT * 16;
+              if (dx == 0 && cc == 0 && fresh) {
+                if (t - 1 >= o1) run(O, t, o1, t - 1, ad, bchunk, 1u);
+                run(O, t, t, t, ad, bchunk, 0u);
+              } else {
+                run(O, t, o1, o2, ad, bchunk, 1u);
+              }
+            }
+          }
+          commit(empty + Lt % WS_RING);  // the input row has fed every output row it feeds
+          if (t >= 2) commit(tfull + (O + t - 2) % NACC);
+        }
+        L += T.rows + 2;
+        O += T.rows;
+      }
+      commit(drain);
+      bool drained = false;
+      for (int it = 0; it < SPIN_LIMIT && !drained; ++it) drained = bar_try(drain, 0u);
+      if (!drained) atomicAdd(&g_conv_timeouts, 1);
+    } else if (!RS && lane == 0) {
       uint32_t L = 0, seen = 0, O = 0;  // rows of the tiles so far, rows waited for, output rows
       bool ok = true;
       for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
@@ -708,8 +796,8 @@ __global__ void __launch_bounds__(WS_THREADS) k_conv3x3_ws(ConvArgs a, int tiles
               ok = false;
               break;
             }
-          const int acc = O % WS_NACC;
-          const uint32_t use = O / WS_NACC;
+          const int acc = O % NACC;
+          const uint32_t use = O / NACC;
           if (ok && use > 0 && !ws_wait(tempty + acc, (use - 1) & 1u, abort_flag)) ok = false;
           if (!ok) break;
           fence_after();
@@ -749,7 +837,7 @@ __global__ void __launch_bounds__(WS_THREADS) k_conv3x3_ws(ConvArgs a, int tiles
     __syncwarp();
   } else {
     // ---- epilogue ----
-    const int ew = warp - 2, quad = warp & 3, half = ew >> 2;
+    const int ew = warp - EPI0, quad = warp & 3, half = ew >> 2;
     uint32_t O = 0;
     bool ok = true;
     for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
@@ -764,15 +852,15 @@ __global__ void __launch_bounds__(WS_THREADS) k_conv3x3_ws(ConvArgs a, int tiles
 #pragma unroll
           for (int q = 0; q < (MODE == 2 ? CH / 8 : 1); ++q) gzv[q] = gp[q];
         }
-        const int acc_i = O % WS_NACC;
-        if (!ws_wait(tfull + acc_i, (O / WS_NACC) & 1u, abort_flag)) {
+        const int acc_i = O % NACC;
+        if (!ws_wait(tfull + acc_i, (O / NACC) & 1u, abort_flag)) {
           ok = false;
           break;
         }
         fence_after();
         float acc[CH];
         {
-          const uint32_t ta = tmem + ((uint32_t)(32 * quad) << 16) + acc_i * TCOLS + half * CH;
+          const uint32_t ta = tmem + ((uint32_t)(32 * quad) << 16) + acc_i * SW + half * CH;
           if (CH == 16) {
             float v[16];
             tld16(ta, v);
@@ -830,7 +918,8 @@ __global__ void __launch_bounds__(WS_THREADS) k_conv3x3_ws(ConvArgs a, int tiles
   fence_before();
   __syncthreads();
   fence_after();
-  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(WS_NACC * TCOLS));
+  if (warp == MMA_WARP)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TALLOC));
 }
 
 }  // namespace tc
@@ -1120,6 +1209,45 @@ int conv_sm_count() {
   return n;
 }
 
+// The warp-specialised kernel's pipeline shape (TEALEAF_GB300_CONV_WS):
+//   0 (default, the measured best) row streaming, a 6-stage ring with 3 rows
+//     ahead, 4 accumulator slots, three blocks per SM;
+//   1 row streaming, an 8-stage ring with 4 rows ahead, 8 slots;
+//   2 the 3-row tile form, an 8-stage ring with 4 stages ahead.
+int conv_ws_cfg() {
+  static const int v = [] {
+    const char *e = getenv("TEALEAF_GB300_CONV_WS");
+    const int k = e ? atoi(e) : 0;
+    return (k >= 0 && k <= 2) ? k : 0;
+  }();
+  return v;
+}
+
+// A persistent grid: as many blocks as fit on the GPU at once (by shared
+// memory), at most one per tile.
+template <int CIN, int COUT, int MODE, class CFG>
+void launch_ws(const ConvArgs &a, cudaStream_t st) {
+  constexpr int smem = tc::SmemWS<CIN, COUT, CFG::RING, CFG::NACC>::BYTES;
+  // blocks per SM: what fits in the 228 KB of shared memory (1 KB reserved
+  // per block) and in the 512 tensor-memory columns
+  constexpr int cols = CFG::RS ? CFG::NACC * COUT : CFG::NACC * tc::TCOLS;
+  constexpr int talloc = cols <= 32 ? 32 : (cols <= 64 ? 64 : (cols <= 128 ? 128 : 256));
+  constexpr int fit = 233472 / (smem + 1024), tfit = 512 / talloc;
+  constexpr int per_sm0 = fit < tfit ? fit : tfit;
+  constexpr int per_sm = per_sm0 < 1 ? 1 : (per_sm0 > 3 ? 3 : per_sm0);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(tc::k_conv3x3_ws<CIN, COUT, MODE, CFG>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(tc::k_conv3x3_ws<CIN, COUT, MODE, CFG>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    attr = true;
+  }
+  const int tiles_x = (a.W + FTP - 1) / FTP, tiles_y = (a.H + tc::WS_ROWS - 1) / tc::WS_ROWS;
+  const long long tiles = (long long)a.N * tiles_x * tiles_y;
+  const long long cap = (long long)per_sm * conv_sm_count();
+  const long long blocks = tiles < cap ? tiles : cap;
+  tc::k_conv3x3_ws<CIN, COUT, MODE, CFG><<<(int)blocks, CFG::THREADS, smem, st>>>(a, tiles_x, tiles_y);
+}
+
 template <int CIN, int COUT, int MODE>
 void launch_conv_mode(const ConvArgs &a, cudaStream_t st) {
   const dim3 grid((a.W + FTP - 1) / FTP, (a.H + FRB - 1) / FRB, a.N);
@@ -1143,16 +1271,11 @@ void launch_conv_mode(const ConvArgs &a, cudaStream_t st) {
     tc::k_conv3x3_tc<CIN, COUT, MODE><<<grid, 256, smem, st>>>(a);
     return;
   }
-  constexpr int smem = tc::SmemWS<CIN, COUT>::BYTES;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(tc::k_conv3x3_ws<CIN, COUT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    attr = true;
+  switch (conv_ws_cfg()) {
+    case 1: launch_ws<CIN, COUT, MODE, tc::WsCfg<8, 4, 1, true>>(a, st); break;
+    case 2: launch_ws<CIN, COUT, MODE, tc::WsCfg<8, 4, 1>>(a, st); break;
+    default: launch_ws<CIN, COUT, MODE, tc::WsCfg<6, 3, 1, true, 4>>(a, st); break;
   }
-  const int tiles_x = (a.W + FTP - 1) / FTP, tiles_y = (a.H + tc::WS_ROWS - 1) / tc::WS_ROWS;
-  const long long tiles = (long long)a.N * tiles_x * tiles_y;
-  const long long blocks = tiles < 2LL * conv_sm_count() ? tiles : 2LL * conv_sm_count();
-  tc::k_conv3x3_ws<CIN, COUT, MODE><<<(int)blocks, tc::WS_THREADS, smem, st>>>(a, tiles_x, tiles_y);
 }
 
 template <int CIN, int COUT>
