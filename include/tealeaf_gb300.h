@@ -313,7 +313,9 @@ typedef struct {
  * mode 0: out = y; 1: out = GELU(y) and z = y (z may be NULL); 2: out = y *
  * GELU'(gz) (input gradient through the previous layer's GELU; b may be NULL).
  * out32 (may be NULL) receives channel 0 of y in FP32.  (cin, cout) in
- * {(16, 32), (32, 32), (32, 16)}.  Runs on the tcgen05 tensor cores
+ * {(16, 32), (32, 32), (32, 16)}.  x, w, gz, z and out must be 16-byte
+ * aligned and out32 4-byte aligned (TL_ERR_ARG otherwise).  Runs on the
+ * tcgen05 tensor cores, the input rows staged by tensor copies
  * (TEALEAF_GB300_CONV=mma selects the warp-level mma.sync kernel). */
 int tl_conv3x3_forward(const void *x, const void *w, const float *bias, const void *gz, void *z, void *out,
                        float *out32, int N, int H, int W, int cin, int cout, int mode, void *stream);

@@ -8,6 +8,8 @@
 // channels contiguous per pixel), zero-padded outside each image.  The three
 // input channels are padded to 16 and the one output channel to 16.  Weights
 // of a layer are [Cout][9][Cin] BF16 (tap = 3*dy + dx), biases FP32.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -75,7 +77,9 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src, int bytes
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(src), "r"(bytes));
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
+// Commits this thread's outstanding copies as a group and waits for all of
+// them (wait_group alone would not cover copies never committed).
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 constexpr int FTP = 128;  // forward: pixels of one image row per block (4 warps x 32)
 constexpr int FRB = 16;   // forward: image rows swept by one block
@@ -535,66 +539,96 @@ __global__ void __launch_bounds__(256) k_conv3x3_tc(ConvArgs a) {
 
 
 // ---------------------------------------------------------------------------
-// Warp-specialised form: the same implicit GEMM, with the producer, the MMA
-// issuer and the epilogue decoupled by mbarriers instead of a block barrier
-// per row.
+// Warp-specialised, row-streaming form: the same implicit GEMM, with the
+// producer, the MMA issuer and the epilogue decoupled by mbarriers.
 // ---------------------------------------------------------------------------
 //
-// A persistent block walks tiles of 128 pixels x WS_ROWS rows (tile t,
-// t + grid, ...).  Ten warps:
-//   warp 0      producer: copies input rows (cp.async) into a ring of
-//               WS_RING staged rows, keeps WS_AHEAD rows in flight, and
-//               publishes a row on its `full` mbarrier once its copies have
-//               landed (each lane waits for its own copies, fences them for
-//               the tensor core's async proxy and arrives);
-//   warp 1      MMA issuer (one lane): waits for the three input rows of an
-//               output row and for a free accumulator, issues the 9 x CIN/16
-//               MMAs into one of WS_NACC tensor-memory accumulators, then
-//               commits the accumulator's `tfull` mbarrier and frees the
-//               input rows no later row needs (`empty`, by tcgen05.commit);
-//   warps 2..9  epilogue: wait for `tfull`, read the accumulator
-//               (tcgen05.ld; lane quadrant warp % 4, channel half
-//               (warp - 2) / 4), release it (`tempty`), then bias, GELU and
-//               the stores.
+// A persistent block walks tiles of 128 pixels x th rows (WsWalk; th is
+// chosen per launch to balance the blocks' work).  Ten warps:
+//   warp 0      producer: stages the input rows y0 - 1 .. y0 + rows of a
+//               tile, in turn, in a ring of RING slots;
+//   warp 1      MMA issuer (one lane), row streaming: each staged input row is
+//               read by the tensor core once per (dx, 16-channel step) with
+//               B = the weights of dy = 2, 1, 0 stacked (N = up to 3 COUT),
+//               accumulating into the up to three output rows it feeds, which
+//               sit in consecutive tensor-memory slots of a ring of NACC; it
+//               then frees the input row (`empty`, by tcgen05.commit) and
+//               hands the output row that is now complete to the epilogue
+//               (`tfull`);
+//   warps 2..9  epilogue: wait for `tfull`, read the accumulator (tcgen05.ld;
+//               lane quadrant warp % 4, channel half (warp - 2) / 4), release
+//               it (`tempty`), then bias, GELU and the stores.
 // Rows stream across tile boundaries, so loads, MMAs and epilogues of
 // neighbouring rows and tiles overlap.  Every mbarrier wait is bounded: one
 // that runs out raises the block's abort flag (every role then leaves its
 // loop) and counts in g_conv_timeouts.
-constexpr int WS_NACC = 4;    // tensor-memory accumulators (TCOLS columns each)
-constexpr int WS_ROWS = 16;   // output rows per tile
-
-// Pipeline shapes: RING staged rows, AHEAD rows in flight before the
-// producer publishes one, NPROD producer warps (10 + NPROD - 1 warps).
-// RS: row streaming.  Each staged input row is read by the tensor core
-// once per (dx, 16-channel step), with N = up to three output rows' channels
-// (the weights of dy = 2, 1, 0 stacked), accumulating into the three output
-// rows it feeds; otherwise each output row reads its three input rows.
-template <int RING_, int AHEAD_, int NPROD_, bool RS_ = false, int NACC_ = (RS_ ? 8 : WS_NACC)>
+//
+// Two producers:
+//   TMA (the default): one thread issues one cp.async.bulk.tensor load per
+//     row (box: CIN channels x 130 pixels, zero-filled outside the image)
+//     that completes on the row's `full` mbarrier.  The row lands as 130
+//     pixel rows of 2 CIN bytes under the 64-byte (CIN 32) or 32-byte (CIN
+//     16) swizzle, which the A descriptors name (K-major, 8-row groups 8 x 2
+//     CIN bytes apart); the tap shift dx is a start address 2 CIN dx bytes on
+//     and the channel step cc one 2 cc bytes on, the swizzle being a function
+//     of the shared-memory address bits.  Slots are 1024-byte aligned.
+//   cp.async: the producer warp's lanes copy 16-byte channel chunks into the
+//     no-swizzle layout [CIN/8 chunks][130 pixels][8 channels], keep AHEAD
+//     rows in flight and publish the oldest (each lane waits for its own
+//     copies, fences them for the tensor core's async proxy and arrives).
+//     The host takes it when the input cannot be described by a tensor map.
+template <int RING_, int AHEAD_, int NACC_, bool TMA_>
 struct WsCfg {
-  static constexpr int RING = RING_, AHEAD = AHEAD_, NPROD = NPROD_;
-  static constexpr bool RS = RS_;
-  static constexpr int NACC = NACC_;             // accumulator slots
-  static_assert(!RS || NACC >= 4, "a row-streaming window holds three slots while one is read");
-  static constexpr int THREADS = 32 * (NPROD + 9);
-  static_assert(RING >= AHEAD + 3, "the ring must hold the rows in flight and the three rows of an MMA");
+  static constexpr int RING = RING_, AHEAD = AHEAD_, NACC = NACC_;
+  static constexpr bool TMA = TMA_;
+  static constexpr int THREADS = 320;
+  static_assert(NACC >= 4, "a row-streaming window holds three slots while one is read");
+  static_assert(TMA ? RING >= 2 : RING >= AHEAD + 1, "the ring must hold the rows in flight and the row read");
 };
 
-template <int CIN, int COUT, int WS_RING, int NACC = WS_NACC>
+template <int CIN, int COUT, class CFG>
 struct SmemWS {
   static constexpr int NC = CIN / 8;
-  static constexpr int ROWB = (FTP + 2) * 16;
-  static constexpr int SLOT = NC * ROWB;
-  static constexpr int KC = 9 * CIN / 8;
-  static constexpr int WB = KC * COUT * 16;
-  static constexpr int BIAS = WB + WS_RING * SLOT;
-  static constexpr int BAR = BIAS + 4 * COUT;                     // 8-byte aligned (SLOT, WB multiples of 16)
-  static constexpr int NBAR = 2 * WS_RING + 2 * NACC + 1;          // full, empty, tfull, tempty, drain
+  static constexpr int ROWB = (FTP + 2) * 16;                      // cp.async: bytes of one channel chunk of a row
+  static constexpr int SLOT = CFG::TMA ? ((FTP + 2) * CIN * 2 + 1023) / 1024 * 1024 : NC * ROWB;
+  static constexpr int WB = 9 * NC * COUT * 16;                    // multiple of 1024
+  static constexpr int BIAS = WB + CFG::RING * SLOT;
+  static constexpr int BAR = BIAS + 4 * COUT;                      // 8-byte aligned
+  static constexpr int NBAR = 2 * CFG::RING + 2 * CFG::NACC + 1;   // full, empty, tfull, tempty, drain
   static constexpr int MISC = BAR + 8 * NBAR;                      // tensor-memory address, abort flag
   static constexpr int BYTES = MISC + 16;
+  static constexpr int ALLOC = BYTES + (CFG::TMA ? 1024 : 0);      // room to align the base to 1024 bytes
+};
+
+// The input of a launch as a tensor map (TMA producer): dimensions
+// {CIN, W, H, N}, box {CIN, 130, 1, 1}.
+struct ConvMaps {
+  CUtensorMap in;
 };
 
 __device__ __forceinline__ void bar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(saddr(bar)) : "memory");
+}
+__device__ __forceinline__ void bar_expect(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(saddr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void tma_load4(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                          uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];\n" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(saddr(bar))
+      : "memory");
+}
+
+// K-major descriptor of a TMA-staged row (pixels of 2 CIN bytes; 64-byte
+// swizzle for CIN 32, 32-byte for CIN 16; 8-row groups 16 CIN bytes apart).
+template <int CIN>
+__device__ __forceinline__ uint64_t sdesc_sw(uint32_t addr) {
+  constexpr uint32_t sbo = 16 * CIN;
+  constexpr uint64_t layout = CIN == 32 ? 4 : 6;
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) |
+         ((uint64_t)1 << 46) | (layout << 61);
 }
 
 // Bounded wait for the completion of `parity`; false (and the abort flag
@@ -608,48 +642,66 @@ __device__ __forceinline__ bool ws_wait(uint64_t *bar, uint32_t parity, volatile
   return false;
 }
 
+// Tiles of 128 pixels x th rows, numbered image, row band, column: block b
+// takes tiles b, b + G, ..., so the GPU sweeps an image band by band and
+// blocks on neighbouring tiles share their halo rows in L2.  Each tile
+// streams its th rows plus the two halo rows.
 struct WsTile {
   int img, x0, y0, rows;
 };
-
-__device__ __forceinline__ WsTile ws_tile(int t, int tiles_x, int tiles_y, int H) {
-  WsTile r;
-  r.img = t / (tiles_x * tiles_y);
-  const int rem = t % (tiles_x * tiles_y);
-  r.x0 = (rem % tiles_x) * FTP;
-  r.y0 = (rem / tiles_x) * WS_ROWS;
-  r.rows = min(WS_ROWS, H - r.y0);
-  return r;
-}
+struct WsWalk {
+  long long t, ntiles;
+  int G, tiles_x, tiles_y, th, H;
+  __device__ WsWalk(int b, int G_, int N, int tiles_x_, int H_, int th_) {
+    tiles_x = tiles_x_;
+    th = th_;
+    H = H_;
+    tiles_y = (H_ + th_ - 1) / th_;
+    ntiles = (long long)N * tiles_x_ * tiles_y;
+    t = b;
+    G = G_;
+  }
+  __device__ bool next(WsTile &s) {
+    if (t >= ntiles) return false;
+    const long long per_img = (long long)tiles_x * tiles_y;
+    const long long img = t / per_img, rem = t - img * per_img;
+    const int band = (int)(rem / tiles_x), tx = (int)(rem - (long long)band * tiles_x);
+    s.img = (int)img;
+    s.x0 = tx * FTP;
+    s.y0 = band * th;
+    s.rows = min(th, H - s.y0);
+    t += G;
+    return true;
+  }
+};
 
 template <int CIN, int COUT, int MODE, class CFG>
-__global__ void __launch_bounds__(CFG::THREADS) k_conv3x3_ws(ConvArgs a, int tiles_x, int tiles_y) {
-  constexpr int WS_RING = CFG::RING, WS_AHEAD = CFG::AHEAD, NPROD = CFG::NPROD, WS_THREADS = CFG::THREADS;
-  constexpr int MMA_WARP = NPROD, EPI0 = NPROD + 1;
-  constexpr bool RS = CFG::RS;
-  constexpr int NACC = CFG::NACC;
-  constexpr int SW = RS ? COUT : TCOLS;                           // tensor-memory columns per accumulator slot
+__global__ void __launch_bounds__(CFG::THREADS) k_conv3x3_ws(ConvArgs a, int tiles_x, int th,
+                                                             const __grid_constant__ ConvMaps maps) {
+  constexpr int RING = CFG::RING, NACC = CFG::NACC, THREADS = CFG::THREADS;
+  constexpr int MMA_WARP = 1, EPI0 = 2;
+  constexpr int SW = COUT;  // tensor-memory columns per accumulator slot
   constexpr int TALLOC = NACC * SW <= 32 ? 32 : (NACC * SW <= 64 ? 64 : (NACC * SW <= 128 ? 128 : 256));
-  using S = SmemWS<CIN, COUT, WS_RING, NACC>;
-  static_assert(COUT % 16 == 0 && COUT <= TCOLS && CIN % 16 == 0, "tile shape");
-  constexpr uint32_t ID = idesc(128, COUT);
+  using S = SmemWS<CIN, COUT, CFG>;
+  static_assert(COUT % 16 == 0 && COUT <= TCOLS && CIN % 16 == 0 && CIN <= 32, "tile shape");
   constexpr int CH = COUT / 2;
-  extern __shared__ __align__(128) unsigned char smem[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char *smem = smem_raw;
+  if constexpr (CFG::TMA) smem += (1024u - (saddr(smem_raw) & 1023u)) & 1023u;
   unsigned char *sw = smem;
   unsigned char *sx = smem + S::WB;
   float *sbias = reinterpret_cast<float *>(smem + S::BIAS);
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + S::BAR);
-  uint64_t *full = bars, *empty = bars + WS_RING, *tfull = bars + 2 * WS_RING, *tempty = tfull + NACC;
+  uint64_t *full = bars, *empty = bars + RING, *tfull = bars + 2 * RING, *tempty = tfull + NACC;
   uint64_t *drain = tempty + NACC;
   uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + S::MISC);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + S::MISC + 4);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int ntiles = a.N * tiles_x * tiles_y;
   const size_t plane = (size_t)a.H * a.W;
 
   if (tid == 0) {
-    for (int k = 0; k < WS_RING; ++k) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(saddr(full + k)), "r"(32 * NPROD));
+    for (int k = 0; k < RING; ++k) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(saddr(full + k)), "r"(CFG::TMA ? 1 : 32));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(empty + k)));
     }
     for (int k = 0; k < NACC; ++k) {
@@ -666,20 +718,13 @@ __global__ void __launch_bounds__(CFG::THREADS) k_conv3x3_ws(ConvArgs a, int til
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
   }
   if (tid < COUT) sbias[tid] = a.bias ? a.bias[tid] : 0.f;
-  if constexpr (RS) {
-    // [dx][k chunk][dy = 2, 1, 0][COUT][8 k values]: the B operand of an
-    // input row's (dx, channel step) MMA, up to three output rows stacked
-    for (int v = tid; v < 9 * S::NC * COUT; v += WS_THREADS) {
-      const int co = v % COUT, d = (v / COUT) % 3, kc = (v / (3 * COUT)) % S::NC, dx = v / (3 * COUT * S::NC);
-      const int tap = 3 * (2 - d) + dx;
-      cp_async16(sw + (((dx * S::NC + kc) * 3 + d) * COUT + co) * 16, a.w + (size_t)co * 9 * CIN + tap * CIN + kc * 8,
-                 16);
-    }
-  } else {
-    for (int v = tid; v < COUT * S::KC; v += WS_THREADS) {
-      const int co = v / S::KC, kc = v % S::KC;
-      cp_async16(sw + (kc * COUT + co) * 16, a.w + (size_t)co * 9 * CIN + kc * 8, 16);
-    }
+  // weights [dx][k chunk][dy = 2, 1, 0][COUT][8 k values]: the B operand of an
+  // input row's (dx, channel step) MMA, up to three output rows stacked
+  for (int v = tid; v < 9 * S::NC * COUT; v += THREADS) {
+    const int co = v % COUT, d = (v / COUT) % 3, kc = (v / (3 * COUT)) % S::NC, dx = v / (3 * COUT * S::NC);
+    const int tap = 3 * (2 - d) + dx;
+    cp_async16(sw + (((dx * S::NC + kc) * 3 + d) * COUT + co) * 16, a.w + (size_t)co * 9 * CIN + tap * CIN + kc * 8,
+               16);
   }
   cp_async_wait_all();
   fence_async_smem();
@@ -689,43 +734,74 @@ __global__ void __launch_bounds__(CFG::THREADS) k_conv3x3_ws(ConvArgs a, int til
   const uint32_t tmem = *tslot;
   const uint32_t wbase = saddr(sw), xbase = saddr(sx);
 
-  if (warp < NPROD) {
-    // ---- producers: warp w copies pixels-chunks w*32 + lane, step 32 * NPROD ----
-    uint32_t L = 0, pub = 0;  // rows issued, rows published
-    bool ok = true;
-    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-      const WsTile T = ws_tile(t, tiles_x, tiles_y, a.H);
-      const bf16 *xi = a.x + (size_t)T.img * plane * CIN;
-      for (int r = 0; r < T.rows + 2 && ok; ++r, ++L) {
-        const int slot = L % WS_RING;
-        const uint32_t use = L / WS_RING;
-        if (use > 0 && !ws_wait(empty + slot, (use - 1) & 1u, abort_flag)) {
-          ok = false;
-          break;
+  if (warp == 0) {
+    if constexpr (CFG::TMA) {
+      // ---- producer: one tensor copy per row ----
+      if (lane == 0) {
+        uint32_t L = 0;  // rows issued
+        bool ok = true;
+        WsWalk walk(blockIdx.x, gridDim.x, a.N, tiles_x, a.H, th);
+        WsTile T;
+        while (ok && walk.next(T)) {
+          for (int r = 0; r < T.rows + 2; ++r, ++L) {
+            const int slot = L % RING;
+            const uint32_t use = L / RING;
+            if (use > 0 && !ws_wait(empty + slot, (use - 1) & 1u, abort_flag)) {
+              ok = false;
+              break;
+            }
+            bar_expect(full + slot, (FTP + 2) * CIN * 2);
+            tma_load4(xbase + slot * S::SLOT, &maps.in, 0, T.x0 - 1, T.y0 - 1 + r, T.img, full + slot);
+          }
         }
-        const int yy = T.y0 - 1 + r;
-        unsigned char *dst = sx + slot * S::SLOT;
-        for (int v = lane + 32 * warp; v < (FTP + 2) * S::NC; v += 32 * NPROD) {
-          const int col = v / S::NC, c8 = v % S::NC, xx = T.x0 + col - 1;
-          const bool in = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
-          const bf16 *src = in ? xi + ((size_t)yy * a.W + xx) * CIN + c8 * 8 : xi;
-          cp_async16(dst + c8 * S::ROWB + col * 16, src, in ? 16 : 0);
-        }
-        cp_async_commit();
-        if (L + 1 - pub > (uint32_t)WS_AHEAD) {  // publish the oldest row in flight
-          asm volatile("cp.async.wait_group %0;\n" ::"n"(WS_AHEAD) : "memory");
-          fence_async_smem();
-          bar_arrive(full + pub % WS_RING);
-          ++pub;
+        // every copy issued has landed before the block leaves (bounded; the
+        // last use of each slot is the one to wait for)
+        for (uint32_t k = L > (uint32_t)RING ? L - RING : 0; k < L; ++k) {
+          bool done = false;
+          for (int it = 0; it < SPIN_LIMIT && !done; ++it) done = bar_try(full + k % RING, (k / RING) & 1u);
+          if (!done) atomicAdd(&g_conv_timeouts, 1);
         }
       }
+      __syncwarp();
+    } else {
+      // ---- producer: lanes copy 16-byte channel chunks ----
+      uint32_t L = 0, pub = 0;  // rows issued, rows published
+      bool ok = true;
+      WsWalk walk(blockIdx.x, gridDim.x, a.N, tiles_x, a.H, th);
+      WsTile T;
+      while (ok && walk.next(T)) {
+        const bf16 *xi = a.x + (size_t)T.img * plane * CIN;
+        for (int r = 0; r < T.rows + 2 && ok; ++r, ++L) {
+          const int slot = L % RING;
+          const uint32_t use = L / RING;
+          if (use > 0 && !ws_wait(empty + slot, (use - 1) & 1u, abort_flag)) {
+            ok = false;
+            break;
+          }
+          const int yy = T.y0 - 1 + r;
+          unsigned char *dst = sx + slot * S::SLOT;
+          for (int v = lane; v < (FTP + 2) * S::NC; v += 32) {
+            const int col = v / S::NC, c8 = v % S::NC, xx = T.x0 + col - 1;
+            const bool in = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
+            const bf16 *src = in ? xi + ((size_t)yy * a.W + xx) * CIN + c8 * 8 : xi;
+            cp_async16(dst + c8 * S::ROWB + col * 16, src, in ? 16 : 0);
+          }
+          cp_async_commit();
+          if (L + 1 - pub > (uint32_t)CFG::AHEAD) {  // publish the oldest row in flight
+            asm volatile("cp.async.wait_group %0;\n" ::"n"(CFG::AHEAD) : "memory");
+            fence_async_smem();
+            bar_arrive(full + pub % RING);
+            ++pub;
+          }
+        }
+      }
+      cp_async_wait_all();
+      fence_async_smem();
+      for (; pub < L; ++pub) bar_arrive(full + pub % RING);
     }
-    cp_async_wait_all();
-    fence_async_smem();
-    for (; pub < L; ++pub) bar_arrive(full + pub % WS_RING);
   } else if (warp == MMA_WARP) {
     // ---- MMA issuer ----
-    if (RS && lane == 0) {
+    if (lane == 0) {
       // one pass per staged input row t of a tile (image row y0 - 1 + t): it
       // feeds output rows t - 2 (dy = 2), t - 1 (dy = 1) and t (dy = 0) of the
       // tile, whose accumulators sit in consecutive slots; out(t) starts here
@@ -741,11 +817,12 @@ __global__ void __launch_bounds__(CFG::THREADS) k_conv3x3_ws(ConvArgs a, int til
         if (c1 < cnt)
           mma(tmem, ad, sdesc(bchunk + (d0 + c1) * COUT * 16, 3 * COUT * 16, 128), idesc(128, (cnt - c1) * COUT), acc);
       };
-      for (int tt = blockIdx.x; tt < ntiles && ok; tt += gridDim.x) {
-        const WsTile T = ws_tile(tt, tiles_x, tiles_y, a.H);
+      WsWalk walk(blockIdx.x, gridDim.x, a.N, tiles_x, a.H, th);
+      WsTile T;
+      while (ok && walk.next(T)) {
         for (int t = 0; t < T.rows + 2; ++t) {
           const uint32_t Lt = L + t;
-          if (!ws_wait(full + Lt % WS_RING, (Lt / WS_RING) & 1u, abort_flag)) {
+          if (!ws_wait(full + Lt % RING, (Lt / RING) & 1u, abort_flag)) {
             ok = false;
             break;
           }
@@ -759,12 +836,13 @@ __global__ void __launch_bounds__(CFG::THREADS) k_conv3x3_ws(ConvArgs a, int til
             }
           }
           fence_after();
-          const uint32_t rbase = xbase + (Lt % WS_RING) * S::SLOT;
+          const uint32_t rbase = xbase + (Lt % RING) * S::SLOT;
 #pragma unroll
           for (int dx = 0; dx < 3; ++dx) {
 #pragma unroll
             for (int cc = 0; cc < CIN; cc += 16) {
-              const uint64_t ad = sdesc(rbase + (cc / 8) * S::ROWB + dx * 16, S::ROWB, 128);
+              const uint64_t ad = CFG::TMA ? sdesc_sw<CIN>(rbase + dx * CIN * 2 + cc * 2)
+                                           : sdesc(rbase + (cc / 8) * S::ROWB + dx * 16, S::ROWB, 128);
               const uint32_t bchunk = wbase + (dx * S::NC + cc / 8) * 3 * COUT * 16;
               if (dx == 0 && cc == 0 && fresh) {
                 if (t - 1 >= o1) run(O, t, o1, t - 1, ad, bchunk, 1u);
@@ -774,58 +852,11 @@ __global__ void __launch_bounds__(CFG::THREADS) k_conv3x3_ws(ConvArgs a, int til
               }
             }
           }
-          commit(empty + Lt % WS_RING);  // the input row has fed every output row it feeds
+          commit(empty + Lt % RING);  // the input row has fed every output row it feeds
           if (t >= 2) commit(tfull + (O + t - 2) % NACC);
         }
         L += T.rows + 2;
         O += T.rows;
-      }
-      commit(drain);
-      bool drained = false;
-      for (int it = 0; it < SPIN_LIMIT && !drained; ++it) drained = bar_try(drain, 0u);
-      if (!drained) atomicAdd(&g_conv_timeouts, 1);
-    } else if (!RS && lane == 0) {
-      uint32_t L = 0, seen = 0, O = 0;  // rows of the tiles so far, rows waited for, output rows
-      bool ok = true;
-      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-        const WsTile T = ws_tile(t, tiles_x, tiles_y, a.H);
-        const uint32_t base = L;
-        for (int i = 0; i < T.rows; ++i, ++O) {
-          for (; seen <= base + i + 2; ++seen)
-            if (!ws_wait(full + seen % WS_RING, (seen / WS_RING) & 1u, abort_flag)) {
-              ok = false;
-              break;
-            }
-          const int acc = O % NACC;
-          const uint32_t use = O / NACC;
-          if (ok && use > 0 && !ws_wait(tempty + acc, (use - 1) & 1u, abort_flag)) ok = false;
-          if (!ok) break;
-          fence_after();
-          const uint32_t d = tmem + acc * TCOLS;
-#pragma unroll
-          for (int dy = 0; dy < 3; ++dy) {
-            const uint32_t rbase = xbase + ((base + i + dy) % WS_RING) * S::SLOT;
-#pragma unroll
-            for (int dx = 0; dx < 3; ++dx) {
-              const int tap = 3 * dy + dx;
-#pragma unroll
-              for (int cc = 0; cc < CIN; cc += 16) {
-                const uint64_t ad = sdesc(rbase + (cc / 8) * S::ROWB + dx * 16, S::ROWB, 128);
-                const uint64_t bd = sdesc(wbase + ((tap * CIN + cc) / 8) * COUT * 16, COUT * 16, 128);
-                mma(d, ad, bd, ID, (tap | cc) != 0);
-              }
-            }
-          }
-          commit(tfull + acc);
-          // input row base + i is needed by no later output row of this tile;
-          // after the tile's last row its two bottom rows are free as well
-          commit(empty + (base + i) % WS_RING);
-          if (i == T.rows - 1) {
-            commit(empty + (base + i + 1) % WS_RING);
-            commit(empty + (base + i + 2) % WS_RING);
-          }
-        }
-        L += T.rows + 2;
       }
       // every MMA issued has completed before the block leaves (bounded, and
       // waited for even after an abort: tensor memory is freed below)
@@ -840,8 +871,9 @@ __global__ void __launch_bounds__(CFG::THREADS) k_conv3x3_ws(ConvArgs a, int til
     const int ew = warp - EPI0, quad = warp & 3, half = ew >> 2;
     uint32_t O = 0;
     bool ok = true;
-    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-      const WsTile T = ws_tile(t, tiles_x, tiles_y, a.H);
+    WsWalk walk(blockIdx.x, gridDim.x, a.N, tiles_x, a.H, th);
+    WsTile T;
+    while (ok && walk.next(T)) {
       const int xx = T.x0 + 32 * quad + lane;
       for (int i = 0; i < T.rows; ++i, ++O) {
         const int y = T.y0 + i;
@@ -1209,11 +1241,13 @@ int conv_sm_count() {
   return n;
 }
 
-// The warp-specialised kernel's pipeline shape (TEALEAF_GB300_CONV_WS):
-//   0 (default, the measured best) row streaming, a 6-stage ring with 3 rows
-//     ahead, 4 accumulator slots, three blocks per SM;
-//   1 row streaming, an 8-stage ring with 4 rows ahead, 8 slots;
-//   2 the 3-row tile form, an 8-stage ring with 4 stages ahead.
+// The warp-specialised kernel's producer and occupancy (TEALEAF_GB300_CONV_WS):
+//   0 (default, the measured best) a tensor copy per row into a 4-slot ring,
+//     three blocks per SM;
+//   1 the same, four blocks per SM;
+//   2 cp.async channel chunks into a 6-slot ring with 3 rows ahead, three
+//     blocks per SM (also taken when the input admits no tensor map).
+// All keep 4 accumulator slots.
 int conv_ws_cfg() {
   static const int v = [] {
     const char *e = getenv("TEALEAF_GB300_CONV_WS");
@@ -1223,29 +1257,80 @@ int conv_ws_cfg() {
   return v;
 }
 
+// cuTensorMapEncodeTiled from the driver, looked up once.
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  }();
+  return fn;
+}
+
+// The input as a 4-D tensor map {CIN, W, H, N} (pixel strides 2 CIN bytes)
+// with box {CIN, FTP + 2, 1, 1}, zero fill outside, the 64-byte (CIN 32) or
+// 32-byte (CIN 16) swizzle; false when it cannot be made.
+template <int CIN>
+bool input_map(const ConvArgs &a, CUtensorMap *m) {
+  const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc || (reinterpret_cast<uintptr_t>(a.x) & 15u) != 0) return false;
+  const cuuint64_t dims[4] = {(cuuint64_t)CIN, (cuuint64_t)a.W, (cuuint64_t)a.H, (cuuint64_t)a.N};
+  const cuuint64_t strides[3] = {(cuuint64_t)CIN * 2, (cuuint64_t)a.W * CIN * 2, (cuuint64_t)a.H * a.W * CIN * 2};
+  const cuuint32_t box[4] = {(cuuint32_t)CIN, (cuuint32_t)(FTP + 2), 1, 1}, es[4] = {1, 1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(a.x), dims, strides, box, es,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CIN == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // A persistent grid: as many blocks as fit on the GPU at once (by shared
-// memory), at most one per tile.
-template <int CIN, int COUT, int MODE, class CFG>
-void launch_ws(const ConvArgs &a, cudaStream_t st) {
-  constexpr int smem = tc::SmemWS<CIN, COUT, CFG::RING, CFG::NACC>::BYTES;
+// memory and tensor memory, at most MAXB per SM), at most one per tile.
+template <int CIN, int COUT, int MODE, class CFG, int MAXB>
+void launch_ws(const ConvArgs &a, const tc::ConvMaps &maps, cudaStream_t st) {
+  constexpr int smem = tc::SmemWS<CIN, COUT, CFG>::ALLOC;
   // blocks per SM: what fits in the 228 KB of shared memory (1 KB reserved
   // per block) and in the 512 tensor-memory columns
-  constexpr int cols = CFG::RS ? CFG::NACC * COUT : CFG::NACC * tc::TCOLS;
+  constexpr int cols = CFG::NACC * COUT;
   constexpr int talloc = cols <= 32 ? 32 : (cols <= 64 ? 64 : (cols <= 128 ? 128 : 256));
   constexpr int fit = 233472 / (smem + 1024), tfit = 512 / talloc;
   constexpr int per_sm0 = fit < tfit ? fit : tfit;
-  constexpr int per_sm = per_sm0 < 1 ? 1 : (per_sm0 > 3 ? 3 : per_sm0);
+  constexpr int per_sm = per_sm0 < 1 ? 1 : (per_sm0 > MAXB ? MAXB : per_sm0);
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(tc::k_conv3x3_ws<CIN, COUT, MODE, CFG>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaFuncSetAttribute(tc::k_conv3x3_ws<CIN, COUT, MODE, CFG>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     attr = true;
   }
-  const int tiles_x = (a.W + FTP - 1) / FTP, tiles_y = (a.H + tc::WS_ROWS - 1) / tc::WS_ROWS;
-  const long long tiles = (long long)a.N * tiles_x * tiles_y;
+  const int tiles_x = (a.W + FTP - 1) / FTP;
   const long long cap = (long long)per_sm * conv_sm_count();
-  const long long blocks = tiles < cap ? tiles : cap;
-  tc::k_conv3x3_ws<CIN, COUT, MODE, CFG><<<(int)blocks, CFG::THREADS, smem, st>>>(a, tiles_x, tiles_y);
+  // tile height: 16 rows when that gives every block slot a tile (measured
+  // best: a short last wave costs less than the halo rows of shorter tiles,
+  // the blocks left on an SM taking its whole bandwidth); on smaller images
+  // the height whose last block finishes first, counting each tile's rows
+  // plus its two halo rows (ties to the taller tile); or the height
+  // TEALEAF_GB300_CONV_ROWS names (1..16)
+  static const int rows_env = [] {
+    const char *e = getenv("TEALEAF_GB300_CONV_ROWS");
+    const int k = e ? atoi(e) : 0;
+    return (k >= 1 && k <= 16) ? k : 0;
+  }();
+  int th = 16;
+  long long best = -1, blocks = 1;
+  const bool full = (long long)a.N * tiles_x * ((a.H + 15) / 16) >= cap;
+  for (int h = 16; h >= 1; --h) {
+    if (rows_env ? h != rows_env : (full && h != 16)) continue;
+    const long long tiles = (long long)a.N * tiles_x * ((a.H + h - 1) / h);
+    const long long g = tiles < cap ? tiles : cap;
+    const long long cost = (tiles + g - 1) / g * (h + 2);
+    if (best < 0 || cost < best) {
+      best = cost;
+      th = h;
+      blocks = g;
+    }
+  }
+  tc::k_conv3x3_ws<CIN, COUT, MODE, CFG><<<(int)blocks, CFG::THREADS, smem, st>>>(a, tiles_x, th, maps);
 }
 
 template <int CIN, int COUT, int MODE>
@@ -1271,10 +1356,16 @@ void launch_conv_mode(const ConvArgs &a, cudaStream_t st) {
     tc::k_conv3x3_tc<CIN, COUT, MODE><<<grid, 256, smem, st>>>(a);
     return;
   }
-  switch (conv_ws_cfg()) {
-    case 1: launch_ws<CIN, COUT, MODE, tc::WsCfg<8, 4, 1, true>>(a, st); break;
-    case 2: launch_ws<CIN, COUT, MODE, tc::WsCfg<8, 4, 1>>(a, st); break;
-    default: launch_ws<CIN, COUT, MODE, tc::WsCfg<6, 3, 1, true, 4>>(a, st); break;
+  using TmaCfg = tc::WsCfg<4, 1, 4, true>;
+  using CpCfg = tc::WsCfg<6, 3, 4, false>;
+  tc::ConvMaps maps;
+  memset(&maps, 0, sizeof(maps));
+  const int cfg = conv_ws_cfg();
+  if (cfg != 2 && input_map<CIN>(a, &maps.in)) {
+    if (cfg == 1) launch_ws<CIN, COUT, MODE, TmaCfg, 4>(a, maps, st);
+    else launch_ws<CIN, COUT, MODE, TmaCfg, 3>(a, maps, st);
+  } else {
+    launch_ws<CIN, COUT, MODE, CpCfg, 3>(a, maps, st);
   }
 }
 
@@ -1291,8 +1382,13 @@ int tl_conv_forward(const void *x, const void *w, const float *bias, const void 
                     int N, int H, int W, int cin, int cout, int mode, cudaStream_t st) {
   if (!x || !w || (!out && !out32) || N < 1 || H < 1 || W < 1 || mode < 0 || mode > 2) return TL_ERR_ARG;
   if (mode == 2 && !gz) return TL_ERR_ARG;
+  // the kernels move activations and weights in 16-byte vectors
+  auto misaligned = [](const void *q, uintptr_t m) { return (reinterpret_cast<uintptr_t>(q) & m) != 0; };
+  if (misaligned(x, 15) || misaligned(w, 15) || misaligned(gz, 15) || misaligned(z, 15) || misaligned(out, 15) ||
+      misaligned(out32, 3))
+    return TL_ERR_ARG;
   if (N > 65535 || (H + FRB - 1) / FRB > 65535) return TL_ERR_ARG;
-  if ((long long)N * ((W + FTP - 1) / FTP) * ((H + tc::WS_ROWS - 1) / tc::WS_ROWS) > 2147483647LL) return TL_ERR_ARG;
+  if ((long long)N * ((W + FTP - 1) / FTP) * H > (1LL << 40)) return TL_ERR_ARG;
   ConvArgs a;
   a.x = static_cast<const bf16 *>(x);
   a.w = static_cast<const bf16 *>(w);

@@ -10,6 +10,9 @@ at the same points) agrees per layer to 5e-2 in norm: a different FP32
 summation order can flip a BF16 rounding, which then propagates.
 """
 import ctypes
+import os
+import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -289,12 +292,14 @@ def test_trained_network_gain(tl, built_lib):
     assert tot["history"] < tot["extrapolate"]
 
 
+@pytest.mark.parametrize("N,H,Wd", [(2, 37, 150), (3, 131, 300), (1, 1040, 1000)])
 @pytest.mark.parametrize("cin,cout,mode", [(16, 32, 1), (32, 32, 1), (32, 16, 0), (32, 32, 2), (16, 32, 0)])
-def test_conv_forward_ragged_shapes(tl, built_lib, cin, cout, mode):
-    """The forward kernel on images whose width spans two 128-pixel segments
-    with a ragged end and whose height is not a multiple of the 16-row sweep,
-    two images, every mode: against the oracle's convolution."""
-    N, H, Wd = 2, 37, 150
+def test_conv_forward_ragged_shapes(tl, built_lib, cin, cout, mode, N, H, Wd):
+    """The forward kernel on images whose width spans 128-pixel columns with
+    a ragged end, several images, every mode, against the oracle's
+    convolution.  The two small shapes get short tiles (one row on 37 x 150 x
+    2), 1040 x 1000 the 16-row tiles with some blocks taking two; the rows
+    are ragged at the bottom of each image."""
     rng = np.random.default_rng(cin * 7 + cout + mode)
     x = W.bf16(rng.standard_normal((N, H, Wd, cin)))
     w = W.bf16(0.1 * rng.standard_normal((cout, 9, cin)))
@@ -322,6 +327,21 @@ def test_conv_forward_ragged_shapes(tl, built_lib, cin, cout, mode):
     assert np.max(np.abs(gg - z[..., 0])) <= 1e-5 * np.max(np.abs(z[..., 0]))
     timeouts = ctypes.c_int(-1)
     assert lib.tl_conv_status(ctypes.byref(timeouts)) == 0 and timeouts.value == 0
+
+
+@pytest.mark.parametrize("knob,value", [("TEALEAF_GB300_CONV_WS", "1"), ("TEALEAF_GB300_CONV_WS", "2"),
+                                        ("TEALEAF_GB300_CONV_ROWS", "1"), ("TEALEAF_GB300_CONV_ROWS", "16")])
+def test_conv_forward_other_producers(built_lib, knob, value):
+    """The same ragged-shape checks in a child process (the choices are read
+    once per process) with the tensor-copy producer at four blocks per SM
+    (CONV_WS 1), with the cp.async producer (CONV_WS 2), with one-row tiles
+    (several per block, streamed back to back) and with 16-row tiles on every
+    shape."""
+    env = dict(os.environ, **{knob: value})
+    r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-p", "no:cacheprovider", "-m", "gpu",
+                        f"{__file__}::test_conv_forward_ragged_shapes"], env=env, capture_output=True, text=True,
+                       timeout=600, cwd=os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
 
 
 def test_warm_context_destroy_leaves_no_error(tl, built_lib, monkeypatch):
