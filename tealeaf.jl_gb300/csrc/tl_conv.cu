@@ -577,10 +577,15 @@ __global__ void __launch_bounds__(256) k_conv3x3_tc(ConvArgs a) {
 //     rows in flight and publish the oldest (each lane waits for its own
 //     copies, fences them for the tensor core's async proxy and arrives).
 //     The host takes it when the input cannot be described by a tensor map.
-template <int RING_, int AHEAD_, int NACC_, bool TMA_>
+// RP: row-parallel epilogue.  The eight epilogue warps form two groups of
+// four (one per lane quadrant); group g takes the output rows O with O % 2 ==
+// g, each thread all COUT channels of its pixel, so two rows' epilogues run
+// at once.  Otherwise all eight warps take every row, a warp half of the
+// channels.
+template <int RING_, int AHEAD_, int NACC_, bool TMA_, bool RP_ = false>
 struct WsCfg {
   static constexpr int RING = RING_, AHEAD = AHEAD_, NACC = NACC_;
-  static constexpr bool TMA = TMA_;
+  static constexpr bool TMA = TMA_, RP = RP_;
   static constexpr int THREADS = 320;
   static_assert(NACC >= 4, "a row-streaming window holds three slots while one is read");
   static_assert(TMA ? RING >= 2 : RING >= AHEAD + 1, "the ring must hold the rows in flight and the row read");
@@ -676,7 +681,7 @@ struct WsWalk {
 };
 
 template <int CIN, int COUT, int MODE, class CFG>
-__global__ void __launch_bounds__(CFG::THREADS) k_conv3x3_ws(ConvArgs a, int tiles_x, int th,
+__global__ void __launch_bounds__(CFG::THREADS, 3) k_conv3x3_ws(ConvArgs a, int tiles_x, int th,
                                                              const __grid_constant__ ConvMaps maps) {
   constexpr int RING = CFG::RING, NACC = CFG::NACC, THREADS = CFG::THREADS;
   constexpr int MMA_WARP = 1, EPI0 = 2;
@@ -684,7 +689,6 @@ __global__ void __launch_bounds__(CFG::THREADS) k_conv3x3_ws(ConvArgs a, int til
   constexpr int TALLOC = NACC * SW <= 32 ? 32 : (NACC * SW <= 64 ? 64 : (NACC * SW <= 128 ? 128 : 256));
   using S = SmemWS<CIN, COUT, CFG>;
   static_assert(COUT % 16 == 0 && COUT <= TCOLS && CIN % 16 == 0 && CIN <= 32, "tile shape");
-  constexpr int CH = COUT / 2;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char *smem = smem_raw;
   if constexpr (CFG::TMA) smem += (1024u - (saddr(smem_raw) & 1023u)) & 1023u;
@@ -706,7 +710,7 @@ __global__ void __launch_bounds__(CFG::THREADS) k_conv3x3_ws(ConvArgs a, int til
     }
     for (int k = 0; k < NACC; ++k) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(tfull + k)));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 256;\n" ::"r"(saddr(tempty + k)));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(saddr(tempty + k)), "r"(CFG::RP ? 128 : 256));
     }
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(drain)));
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -868,7 +872,9 @@ __global__ void __launch_bounds__(CFG::THREADS) k_conv3x3_ws(ConvArgs a, int til
     __syncwarp();
   } else {
     // ---- epilogue ----
-    const int ew = warp - EPI0, quad = warp & 3, half = ew >> 2;
+    constexpr bool RP = CFG::RP;
+    constexpr int CW = RP ? COUT : COUT / 2;  // channels per thread
+    const int ew = warp - EPI0, quad = warp & 3, grp = ew >> 2, half = RP ? 0 : grp;
     uint32_t O = 0;
     bool ok = true;
     WsWalk walk(blockIdx.x, gridDim.x, a.N, tiles_x, a.H, th);
@@ -876,13 +882,14 @@ __global__ void __launch_bounds__(CFG::THREADS) k_conv3x3_ws(ConvArgs a, int til
     while (ok && walk.next(T)) {
       const int xx = T.x0 + 32 * quad + lane;
       for (int i = 0; i < T.rows; ++i, ++O) {
+        if (RP && (int)(O & 1u) != grp) continue;
         const int y = T.y0 + i;
-        uint4 gzv[MODE == 2 ? CH / 8 : 1];
+        uint4 gzv[MODE == 2 ? CW / 8 : 1];
         if (MODE == 2 && xx < a.W) {
           const uint4 *gp = reinterpret_cast<const uint4 *>(
-              a.gz + ((size_t)T.img * plane + (size_t)y * a.W + xx) * COUT + half * CH);
+              a.gz + ((size_t)T.img * plane + (size_t)y * a.W + xx) * COUT + half * CW);
 #pragma unroll
-          for (int q = 0; q < (MODE == 2 ? CH / 8 : 1); ++q) gzv[q] = gp[q];
+          for (int q = 0; q < (MODE == 2 ? CW / 8 : 1); ++q) gzv[q] = gp[q];
         }
         const int acc_i = O % NACC;
         if (!ws_wait(tfull + acc_i, (O / NACC) & 1u, abort_flag)) {
@@ -890,19 +897,22 @@ __global__ void __launch_bounds__(CFG::THREADS) k_conv3x3_ws(ConvArgs a, int til
           break;
         }
         fence_after();
-        float acc[CH];
+        float acc[CW];
         {
-          const uint32_t ta = tmem + ((uint32_t)(32 * quad) << 16) + acc_i * SW + half * CH;
-          if (CH == 16) {
-            float v[16];
-            tld16(ta, v);
+          const uint32_t ta = tmem + ((uint32_t)(32 * quad) << 16) + acc_i * SW + half * CW;
+          if constexpr (CW >= 16) {
 #pragma unroll
-            for (int k = 0; k < CH; ++k) acc[k] = v[k];
+            for (int c0 = 0; c0 < CW; c0 += 16) {
+              float v[16];
+              tld16(ta + c0, v);
+#pragma unroll
+              for (int k = 0; k < 16; ++k) acc[c0 + k] = v[k];
+            }
           } else {
             float v[8];
             tld8(ta, v);
 #pragma unroll
-            for (int k = 0; k < CH; ++k) acc[k] = v[k];
+            for (int k = 0; k < CW; ++k) acc[k] = v[k];
           }
         }
         fence_before();
@@ -910,11 +920,11 @@ __global__ void __launch_bounds__(CFG::THREADS) k_conv3x3_ws(ConvArgs a, int til
         if (xx < a.W) {
           const size_t pix = (size_t)T.img * plane + (size_t)y * a.W + xx;
 #pragma unroll
-          for (int c = 0; c < CH; ++c) acc[c] += sbias[half * CH + c];
+          for (int c = 0; c < CW; ++c) acc[c] += sbias[half * CW + c];
           if (a.out32 && half == 0) a.out32[pix] = acc[0];
-          uint4 zo[CH / 8], oo[CH / 8];
+          uint4 zo[CW / 8], oo[CW / 8];
 #pragma unroll
-          for (int q = 0; q < CH / 8; ++q) {
+          for (int q = 0; q < CW / 8; ++q) {
             __nv_bfloat162 *zp = reinterpret_cast<__nv_bfloat162 *>(&zo[q]);
             __nv_bfloat162 *op = reinterpret_cast<__nv_bfloat162 *>(&oo[q]);
             const __nv_bfloat162 *gq = reinterpret_cast<const __nv_bfloat162 *>(&gzv[MODE == 2 ? q : 0]);
@@ -934,14 +944,14 @@ __global__ void __launch_bounds__(CFG::THREADS) k_conv3x3_ws(ConvArgs a, int til
             }
           }
           if (MODE == 1 && a.z) {
-            uint4 *zd = reinterpret_cast<uint4 *>(a.z + pix * COUT + half * CH);
+            uint4 *zd = reinterpret_cast<uint4 *>(a.z + pix * COUT + half * CW);
 #pragma unroll
-            for (int q = 0; q < CH / 8; ++q) zd[q] = zo[q];
+            for (int q = 0; q < CW / 8; ++q) zd[q] = zo[q];
           }
           if (a.out) {
-            uint4 *od = reinterpret_cast<uint4 *>(a.out + pix * COUT + half * CH);
+            uint4 *od = reinterpret_cast<uint4 *>(a.out + pix * COUT + half * CW);
 #pragma unroll
-            for (int q = 0; q < CH / 8; ++q) od[q] = oo[q];
+            for (int q = 0; q < CW / 8; ++q) od[q] = oo[q];
           }
         }
       }
@@ -1241,13 +1251,15 @@ int conv_sm_count() {
   return n;
 }
 
-// The warp-specialised kernel's producer and occupancy (TEALEAF_GB300_CONV_WS):
-//   0 (default, the measured best) a tensor copy per row into a 4-slot ring,
-//     three blocks per SM;
-//   1 the same, four blocks per SM;
-//   2 cp.async channel chunks into a 6-slot ring with 3 rows ahead, three
-//     blocks per SM (also taken when the input admits no tensor map).
-// All keep 4 accumulator slots.
+// The warp-specialised kernel's producer and epilogue (TEALEAF_GB300_CONV_WS):
+//   0 (default) a tensor copy per row into a 4-slot ring, row-parallel
+//     epilogue for the forward modes (0, 1), every epilogue warp on every
+//     row for the input gradient (2: its gz loads measured slower per pixel);
+//   1 the same with every epilogue warp on every row (half the channels);
+//   2 cp.async channel chunks into a 6-slot ring with 3 rows ahead, every
+//     epilogue warp on every row (also taken when the input admits no
+//     tensor map).
+// All keep 4 accumulator slots and at most three blocks per SM.
 int conv_ws_cfg() {
   static const int v = [] {
     const char *e = getenv("TEALEAF_GB300_CONV_WS");
@@ -1356,13 +1368,14 @@ void launch_conv_mode(const ConvArgs &a, cudaStream_t st) {
     tc::k_conv3x3_tc<CIN, COUT, MODE><<<grid, 256, smem, st>>>(a);
     return;
   }
-  using TmaCfg = tc::WsCfg<4, 1, 4, true>;
+  using TmaCfg = tc::WsCfg<4, 1, 4, true, MODE != 2>;  // the input gradient measured faster on all rows
+  using TmaCfgAll = tc::WsCfg<4, 1, 4, true, false>;
   using CpCfg = tc::WsCfg<6, 3, 4, false>;
   tc::ConvMaps maps;
   memset(&maps, 0, sizeof(maps));
   const int cfg = conv_ws_cfg();
   if (cfg != 2 && input_map<CIN>(a, &maps.in)) {
-    if (cfg == 1) launch_ws<CIN, COUT, MODE, TmaCfg, 4>(a, maps, st);
+    if (cfg == 1) launch_ws<CIN, COUT, MODE, TmaCfgAll, 3>(a, maps, st);
     else launch_ws<CIN, COUT, MODE, TmaCfg, 3>(a, maps, st);
   } else {
     launch_ws<CIN, COUT, MODE, CpCfg, 3>(a, maps, st);
