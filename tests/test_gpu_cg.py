@@ -15,7 +15,7 @@ from parity_util import CONFIG1, FIELDS, deck_text, gpu_run, oracle_run, random_
 pytestmark = pytest.mark.gpu
 
 REF, TEA = O.MODE_REFERENCE, O.MODE_TEALEAF
-SUMMARY_RTOL = 1e-12          # spec field_summary tolerance (FP64)
+SUMMARY_RTOL = 1e-12          # field_summary tolerance, relative (FP64)
 
 
 def _layout(chunk):
