@@ -329,6 +329,29 @@ def test_conv_forward_ragged_shapes(tl, built_lib, cin, cout, mode, N, H, Wd):
     assert lib.tl_conv_status(ctypes.byref(timeouts)) == 0 and timeouts.value == 0
 
 
+def test_conv_forward_at_the_measured_size(tl, built_lib):
+    """The 32->32 GELU layer on one 2048 x 2048 image, the size whose rate
+    the bench reports (16-row tiles, several per block), against the
+    oracle's convolution: every output within one BF16 rounding."""
+    n, ci, co = 2048, 32, 32
+    rng = np.random.default_rng(2048)
+    x = W.bf16(rng.standard_normal((1, n, n, ci)).astype(np.float32))
+    w = W.bf16(0.05 * rng.standard_normal((co, 9, ci)))
+    b = rng.standard_normal(co).astype(np.float32).astype(np.float64)
+    dev = lambda a: torch.tensor(a, dtype=torch.float32, device="cuda").to(torch.bfloat16)  # noqa: E731
+    xd, wd = dev(x), dev(w.reshape(-1))
+    bd = torch.tensor(b, dtype=torch.float32, device="cuda")
+    out = torch.zeros((1, n, n, co), dtype=torch.bfloat16, device="cuda")
+    lib = tl._abi.load()
+    st = torch.cuda.current_stream().cuda_stream
+    assert lib.tl_conv3x3_forward(xd.data_ptr(), wd.data_ptr(), bd.data_ptr(), None, None, out.data_ptr(), None,
+                                  1, n, n, ci, co, 1, st) == 0
+    torch.cuda.synchronize()
+    close_bf16(f64(out), W.bf16(W.gelu(W.conv(x, w) + b)), "conv 32->32 GELU at 2048^2")
+    timeouts = ctypes.c_int(-1)
+    assert lib.tl_conv_status(ctypes.byref(timeouts)) == 0 and timeouts.value == 0
+
+
 @pytest.mark.parametrize("knob,value", [("TEALEAF_GB300_CONV_WS", "1"), ("TEALEAF_GB300_CONV_WS", "2"),
                                         ("TEALEAF_GB300_CONV_ROWS", "1"), ("TEALEAF_GB300_CONV_ROWS", "16")])
 def test_conv_forward_other_producers(built_lib, knob, value):
