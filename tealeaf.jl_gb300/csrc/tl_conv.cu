@@ -582,9 +582,9 @@ __global__ void __launch_bounds__(256) k_conv3x3_tc(ConvArgs a) {
 // g, each thread all COUT channels of its pixel, so two rows' epilogues run
 // at once.  Otherwise all eight warps take every row, a warp half of the
 // channels.
-template <int RING_, int AHEAD_, int NACC_, bool TMA_, bool RP_ = false>
+template <int RING_, int AHEAD_, int NACC_, bool TMA_, bool RP_ = false, int MINB_ = 3>
 struct WsCfg {
-  static constexpr int RING = RING_, AHEAD = AHEAD_, NACC = NACC_;
+  static constexpr int RING = RING_, AHEAD = AHEAD_, NACC = NACC_, MINB = MINB_;
   static constexpr bool TMA = TMA_, RP = RP_;
   static constexpr int THREADS = 320;
   static_assert(NACC >= 4, "a row-streaming window holds three slots while one is read");
@@ -681,7 +681,7 @@ struct WsWalk {
 };
 
 template <int CIN, int COUT, int MODE, class CFG>
-__global__ void __launch_bounds__(CFG::THREADS, 3) k_conv3x3_ws(ConvArgs a, int tiles_x, int th,
+__global__ void __launch_bounds__(CFG::THREADS, CFG::MINB) k_conv3x3_ws(ConvArgs a, int tiles_x, int th,
                                                              const __grid_constant__ ConvMaps maps) {
   constexpr int RING = CFG::RING, NACC = CFG::NACC, THREADS = CFG::THREADS;
   constexpr int MMA_WARP = 1, EPI0 = 2;
@@ -1252,14 +1252,16 @@ int conv_sm_count() {
 }
 
 // The warp-specialised kernel's producer and epilogue (TEALEAF_GB300_CONV_WS):
-//   0 (default) a tensor copy per row into a 4-slot ring, row-parallel
-//     epilogue for the forward modes (0, 1), every epilogue warp on every
-//     row for the input gradient (2: its gz loads measured slower per pixel);
-//   1 the same with every epilogue warp on every row (half the channels);
+//   0 (default) a tensor copy per row into a 4-slot ring; the GELU forward
+//     (mode 1) with the row-parallel epilogue at three blocks per SM, the
+//     plain output (0) and the input gradient (2) with every epilogue warp
+//     on every row at four blocks per SM (each measured best for its mode);
+//   1 a tensor copy per row, every epilogue warp on every row (half the
+//     channels), three blocks per SM, every mode;
 //   2 cp.async channel chunks into a 6-slot ring with 3 rows ahead, every
 //     epilogue warp on every row (also taken when the input admits no
 //     tensor map).
-// All keep 4 accumulator slots and at most three blocks per SM.
+// All keep 4 accumulator slots.
 int conv_ws_cfg() {
   static const int v = [] {
     const char *e = getenv("TEALEAF_GB300_CONV_WS");
@@ -1368,7 +1370,11 @@ void launch_conv_mode(const ConvArgs &a, cudaStream_t st) {
     tc::k_conv3x3_tc<CIN, COUT, MODE><<<grid, 256, smem, st>>>(a);
     return;
   }
-  using TmaCfg = tc::WsCfg<4, 1, 4, true, MODE != 2>;  // the input gradient measured faster on all rows
+  // GELU forward: the row-parallel epilogue at three blocks per SM; plain
+  // output and input gradient: every epilogue warp on every row at four
+  // blocks per SM (registers capped at 48; measured faster for those two)
+  using TmaCfg = tc::WsCfg<4, 1, 4, true, MODE == 1, MODE == 1 ? 3 : 4>;
+  constexpr int TMA_MAXB = MODE == 1 ? 3 : 4;
   using TmaCfgAll = tc::WsCfg<4, 1, 4, true, false>;
   using CpCfg = tc::WsCfg<6, 3, 4, false>;
   tc::ConvMaps maps;
@@ -1376,7 +1382,7 @@ void launch_conv_mode(const ConvArgs &a, cudaStream_t st) {
   const int cfg = conv_ws_cfg();
   if (cfg != 2 && input_map<CIN>(a, &maps.in)) {
     if (cfg == 1) launch_ws<CIN, COUT, MODE, TmaCfgAll, 3>(a, maps, st);
-    else launch_ws<CIN, COUT, MODE, TmaCfg, 3>(a, maps, st);
+    else launch_ws<CIN, COUT, MODE, TmaCfg, TMA_MAXB>(a, maps, st);
   } else {
     launch_ws<CIN, COUT, MODE, CpCfg, 3>(a, maps, st);
   }
