@@ -356,10 +356,10 @@ def test_conv_forward_at_the_measured_size(tl, built_lib):
                                         ("TEALEAF_GB300_CONV_ROWS", "1"), ("TEALEAF_GB300_CONV_ROWS", "16")])
 def test_conv_forward_other_producers(built_lib, knob, value):
     """The same ragged-shape checks in a child process (the choices are read
-    once per process) with the tensor-copy producer at four blocks per SM
-    (CONV_WS 1), with the cp.async producer (CONV_WS 2), with one-row tiles
-    (several per block, streamed back to back) and with 16-row tiles on every
-    shape."""
+    once per process): tensor-copy rows with every epilogue warp on every
+    row at three blocks per SM in every mode (CONV_WS 1), the cp.async
+    producer (CONV_WS 2), one-row tiles (several per block, streamed back to
+    back) and 16-row tiles on every shape."""
     env = dict(os.environ, **{knob: value})
     r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-p", "no:cacheprovider", "-m", "gpu",
                         f"{__file__}::test_conv_forward_ragged_shapes"], env=env, capture_output=True, text=True,
