@@ -325,7 +325,8 @@ int tl_conv3x3_forward(const void *x, const void *w, const float *bias, const vo
  * unwritten), and resets the count. */
 int tl_conv_status(int *timeouts);
 /* dw[cout][9][cin], then db[cout] = the weight and bias gradients; partials
- * holds nparts * (cout*9*cin + cout) floats. */
+ * holds nparts * (cout*9*cin + cout) floats.  x and dz must be 16-byte
+ * aligned (TL_ERR_ARG otherwise). */
 int tl_conv3x3_weight_grad(const void *x, const void *dz, float *partials, int nparts, float *dw, int N, int H, int W,
                            int cin, int cout, void *stream);
 /* wt[ci][tap][co] = w[co][8 - tap][ci]: weights of the input-gradient convolution. */

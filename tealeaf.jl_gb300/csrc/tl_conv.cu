@@ -1444,6 +1444,10 @@ extern "C" int tl_conv_status(int *timeouts) {
 extern "C" int tl_conv3x3_weight_grad(const void *x, const void *dz, float *partials, int nparts, float *dw, int N,
                                       int H, int W, int cin, int cout, void *stream) {
   if (!x || !dz || !partials || !dw || nparts < 1 || N < 1 || H < 1 || W < 1) return TL_ERR_ARG;
+  // activations are read in 16-byte vectors, partials and gradients as floats
+  if ((reinterpret_cast<uintptr_t>(x) & 15u) || (reinterpret_cast<uintptr_t>(dz) & 15u) ||
+      (reinterpret_cast<uintptr_t>(partials) & 3u) || (reinterpret_cast<uintptr_t>(dw) & 3u))
+    return TL_ERR_ARG;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   auto X = static_cast<const bf16 *>(x);
   auto Z = static_cast<const bf16 *>(dz);

@@ -175,3 +175,39 @@ def test_create_rejects_invalid_configurations(tl, built_lib, cfg, code):
     msg = lib.tl_last_error(ctx)
     lib.tl_destroy(ctx)
     assert rc == code and msg
+
+
+# Fake device addresses: the argument checks of tl_conv3x3_forward run before
+# any CUDA call, so nothing here touches a device.
+_A = 1 << 20          # 16-byte aligned
+_CONV_OK = dict(x=_A, w=_A, b=_A, gz=None, z=None, out=_A, out32=None, N=1, H=8, W=8, cin=32, cout=32, mode=1)
+
+
+@pytest.mark.parametrize("change", [
+    dict(x=None), dict(w=None), dict(out=None, out32=None), dict(mode=3), dict(mode=-1), dict(mode=2, gz=None),
+    dict(N=0), dict(H=0), dict(W=0), dict(x=_A + 2), dict(w=_A + 8), dict(out=_A + 4), dict(gz=_A + 1, mode=2),
+    dict(z=_A + 8), dict(out32=_A + 2), dict(cin=16, cout=16), dict(cin=8, cout=32), dict(cin=32, cout=64),
+])
+def test_conv_forward_rejects_invalid_arguments(tl, built_lib, change):
+    """tl_conv3x3_forward returns TL_ERR_ARG, before any launch, for null or
+    misaligned buffers (activations and weights 16-byte, out32 4-byte), an
+    unknown mode, mode 2 without gz, empty images and channel counts outside
+    (16, 32), (32, 32), (32, 16)."""
+    lib = tl._abi.load()
+    a = dict(_CONV_OK, **change)
+    rc = lib.tl_conv3x3_forward(a["x"], a["w"], a["b"], a["gz"], a["z"], a["out"], a["out32"], a["N"], a["H"], a["W"],
+                                a["cin"], a["cout"], a["mode"], None)
+    assert rc == tl._abi.ERR_ARG, change
+
+
+@pytest.mark.parametrize("change", [dict(x=None), dict(x=_A + 2), dict(dz=_A + 8), dict(partials=_A + 2),
+                                    dict(dw=_A + 1), dict(nparts=0), dict(N=0), dict(cin=16, cout=16)])
+def test_conv_weight_grad_rejects_invalid_arguments(tl, built_lib, change):
+    """tl_conv3x3_weight_grad returns TL_ERR_ARG, before any launch, for null
+    or misaligned buffers, no partials, an empty image and unsupported
+    channel counts."""
+    lib = tl._abi.load()
+    a = dict(dict(x=_A, dz=_A, partials=_A, nparts=4, dw=_A, N=1, H=8, W=8, cin=32, cout=32), **change)
+    rc = lib.tl_conv3x3_weight_grad(a["x"], a["dz"], a["partials"], a["nparts"], a["dw"], a["N"], a["H"], a["W"],
+                                    a["cin"], a["cout"], None)
+    assert rc == tl._abi.ERR_ARG, change
